@@ -1,0 +1,77 @@
+/* Internal C ABI between the C host layer (fftset_host.c) and the CUDA
+ * kernels (fgk_*.cu). Plain C structs of sizes, offsets and device pointers;
+ * no torch and no C++ types. Not part of the public interface. */
+#ifndef FGK_H
+#define FGK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FGK_MAX_STAGES 24
+
+/* One Stockham stage of a resident transform of length L.
+ * Butterfly j (0 <= j < L/radix) reads x[j + p L/radix], multiplies input p
+ * by w_{ns*radix}^{p (j mod ns)}, runs DFT_radix and writes output q to
+ * (j - j mod ns) radix + (j mod ns) + q ns. After all stages the sequence is
+ * the natural-order DFT. */
+typedef struct fgk_stage {
+	uint32_t radix;
+	uint32_t ns;      /* product of the radices of the stages before */
+	uint32_t tw_off;  /* float2 offset of this stage's twiddles: (radix-1)*ns entries, [k][p-1] */
+	uint32_t nb;      /* butterflies per thread (ceil(L/radix / threads)) */
+} fgk_stage;
+
+typedef struct fgk_chain {
+	uint32_t  nstages;
+	fgk_stage st[FGK_MAX_STAGES];
+} fgk_chain;
+
+enum fgk_modulation { FGK_MOD_COMPLEX = 0, FGK_MOD_FREQOFF = 1 };
+
+enum fgk_op {
+	FGK_OP_FORWARD = 0,
+	FGK_OP_INVERSE = 1,
+	FGK_OP_KERNEL  = 2,   /* fftset_fft_conv_get_kernel */
+	FGK_OP_CONV    = 3,   /* fftset_fft_conv */
+	FGK_OP_CORR    = 4,   /* convolution with the conjugated kernel spectrum (adjoint w.r.t. input) */
+	FGK_OP_COUNT
+};
+
+/* Device-side plan of one resident (shared-memory) transform. */
+typedef struct fgk_plan {
+	uint32_t  L;           /* complex bins */
+	uint32_t  modulation;  /* enum fgk_modulation */
+	uint32_t  threads;     /* threads per transform */
+	uint32_t  per_cta;     /* transforms per CTA */
+	uint32_t  smem_stride; /* float2 slots of shared memory per transform */
+	uint32_t  kvw;         /* kernel-buffer lane width: imag = real offset + kvw */
+	uint32_t  pad;         /* 1: shared-memory slot of element i is i + i/16; 0: i */
+	uint32_t  emax;        /* register budget (complex elements per thread per stage): 16 or 32 */
+	fgk_chain fwd;         /* natural in -> natural out */
+	fgk_chain inv;         /* fwd's radices reversed: the chain run after the spectrum product */
+	const void    *tw;     /* device float2 twiddles of both chains */
+	const void    *modtw;  /* device float2[L] e^{-j pi i/(2L)} (FREQOFF only) */
+	const int32_t *kidx;   /* device int32[L]: kernel-buffer float offset of bin m's real part */
+	const struct fgk_plan *dev; /* device copy of this struct (kernels index its chains) */
+} fgk_plan;
+
+/* Host-side planning helpers implemented in fgk_plan.c */
+int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
+int  fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes);
+/* Number of float2 twiddles both chains of p need; fills them when tw != NULL. */
+size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2);
+
+/* Launchers implemented in fgk_kernels.cu. All return 0 or a cudaError_t. */
+int fgk_launch_resident(const fgk_plan *p, int op, float *out, const float *in, const float *kern,
+                        uint32_t count, size_t in_stride, size_t out_stride, void *stream);
+uint32_t fgk_max_resident_L(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,199 @@
+/* Register-resident DFT codelets (forward sign, natural order in and out).
+ *
+ * dft<R>(v) replaces v[0..R) by X[k] = sum_p v[p] e^{-j 2 pi p k / R}.
+ * Radices 2, 3, 4, 5, 8 are written out; 16 is 4x4 Cooley-Tukey with its
+ * internal twiddles written as constants; 6, 10, 12 and 15 are Good-Thomas
+ * prime-factor composites (coprime factors, no internal twiddles, the index
+ * maps are compile-time register renamings). These play the role of the
+ * reference's radix butterflies (src/fftset_vec.c:109-845) but are this
+ * project's own GPU codelets: one thread holds a whole butterfly in registers.
+ *
+ * The header also compiles as plain host C++ so the codelets can be unit
+ * tested without a GPU. */
+#pragma once
+
+#ifdef __CUDACC__
+#define FGK_HD __host__ __device__ __forceinline__
+#else
+#define FGK_HD inline
+#include <cmath>
+struct float2 { float x, y; };
+static inline float2 make_float2(float a, float b) { float2 r; r.x = a; r.y = b; return r; }
+#endif
+
+namespace fgk {
+
+FGK_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+FGK_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+FGK_HD float2 cmul(float2 a, float2 w) { return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x); }
+/* a * conj(w) */
+FGK_HD float2 cmulc(float2 a, float2 w) { return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y); }
+FGK_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+/* a * (-j) */
+FGK_HD float2 mul_mj(float2 a) { return make_float2(a.y, -a.x); }
+FGK_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+/* exact decimal expansions of the constants named */
+#define FGK_SQRT1_2 0.70710678118654752440f  /* cos(pi/4) */
+#define FGK_COS_PI8 0.92387953251128675613f  /* cos(pi/8) */
+#define FGK_SIN_PI8 0.38268343236508977173f  /* sin(pi/8) */
+#define FGK_SIN_PI3 0.86602540378443864676f  /* sin(pi/3) */
+#define FGK_C1_5    0.30901699437494742410f  /* cos(2pi/5) */
+#define FGK_C2_5    0.80901699437494742410f  /* -cos(4pi/5) */
+#define FGK_S1_5    0.95105651629515357212f  /* sin(2pi/5) */
+#define FGK_S2_5    0.58778525229247312917f  /* sin(4pi/5) */
+
+FGK_HD void dft2(float2 &a, float2 &b)
+{
+	float2 t = a;
+	a = cadd(t, b);
+	b = csub(t, b);
+}
+
+FGK_HD void dft3(float2 &a, float2 &b, float2 &c)
+{
+	float2 s = cadd(b, c);
+	float2 d = csub(b, c);
+	float2 m = make_float2(a.x - 0.5f * s.x, a.y - 0.5f * s.y);
+	a = cadd(a, s);
+	/* X1 = m - j sin(pi/3) d ; X2 = m + j sin(pi/3) d */
+	b = make_float2(m.x + FGK_SIN_PI3 * d.y, m.y - FGK_SIN_PI3 * d.x);
+	c = make_float2(m.x - FGK_SIN_PI3 * d.y, m.y + FGK_SIN_PI3 * d.x);
+}
+
+FGK_HD void dft4(float2 &a, float2 &b, float2 &c, float2 &d)
+{
+	float2 s0 = cadd(a, c), d0 = csub(a, c);
+	float2 s1 = cadd(b, d), d1 = mul_mj(csub(b, d));
+	a = cadd(s0, s1);
+	c = csub(s0, s1);
+	b = cadd(d0, d1);
+	d = csub(d0, d1);
+}
+
+FGK_HD void dft5(float2 &x0, float2 &x1, float2 &x2, float2 &x3, float2 &x4)
+{
+	float2 s1 = cadd(x1, x4), d1 = csub(x1, x4);
+	float2 s2 = cadd(x2, x3), d2 = csub(x2, x3);
+	float2 a1 = make_float2(x0.x + FGK_C1_5 * s1.x - FGK_C2_5 * s2.x, x0.y + FGK_C1_5 * s1.y - FGK_C2_5 * s2.y);
+	float2 a2 = make_float2(x0.x - FGK_C2_5 * s1.x + FGK_C1_5 * s2.x, x0.y - FGK_C2_5 * s1.y + FGK_C1_5 * s2.y);
+	/* b1 = sin(2pi/5) d1 + sin(4pi/5) d2 ; b2 = sin(4pi/5) d1 - sin(2pi/5) d2 */
+	float2 b1 = make_float2(FGK_S1_5 * d1.x + FGK_S2_5 * d2.x, FGK_S1_5 * d1.y + FGK_S2_5 * d2.y);
+	float2 b2 = make_float2(FGK_S2_5 * d1.x - FGK_S1_5 * d2.x, FGK_S2_5 * d1.y - FGK_S1_5 * d2.y);
+	x0 = cadd(x0, cadd(s1, s2));
+	/* X1 = a1 - j b1, X4 = a1 + j b1, X2 = a2 - j b2, X3 = a2 + j b2 */
+	x1 = make_float2(a1.x + b1.y, a1.y - b1.x);
+	x4 = make_float2(a1.x - b1.y, a1.y + b1.x);
+	x2 = make_float2(a2.x + b2.y, a2.y - b2.x);
+	x3 = make_float2(a2.x - b2.y, a2.y + b2.x);
+}
+
+/* 8 = 2 x 4 decimation in frequency:
+ * u_p = v_p + v_{p+4}, t_p = (v_p - v_{p+4}) w8^p, X[2k] = DFT4(u)[k],
+ * X[2k+1] = DFT4(t)[k]. */
+FGK_HD void dft8(float2 *v)
+{
+	float2 u0 = cadd(v[0], v[4]), t0 = csub(v[0], v[4]);
+	float2 u1 = cadd(v[1], v[5]), t1 = csub(v[1], v[5]);
+	float2 u2 = cadd(v[2], v[6]), t2 = csub(v[2], v[6]);
+	float2 u3 = cadd(v[3], v[7]), t3 = csub(v[3], v[7]);
+	/* w8^1 = (1-j)/sqrt2, w8^2 = -j, w8^3 = -(1+j)/sqrt2 */
+	t1 = make_float2(FGK_SQRT1_2 * (t1.x + t1.y), FGK_SQRT1_2 * (t1.y - t1.x));
+	t2 = mul_mj(t2);
+	t3 = make_float2(FGK_SQRT1_2 * (t3.y - t3.x), -FGK_SQRT1_2 * (t3.x + t3.y));
+	dft4(u0, u1, u2, u3);
+	dft4(t0, t1, t2, t3);
+	v[0] = u0; v[2] = u1; v[4] = u2; v[6] = u3;
+	v[1] = t0; v[3] = t1; v[5] = t2; v[7] = t3;
+}
+
+/* 16 = 4 x 4: column DFT4 over p2 of v[p1 + 4 p2], twiddle w16^{p1 k2},
+ * row DFT4 over p1, X[4 k1 + k2]. */
+FGK_HD void dft16(float2 *v)
+{
+	float2 c[4][4];
+#pragma unroll
+	for (int p1 = 0; p1 < 4; p1++) {
+		c[p1][0] = v[p1];
+		c[p1][1] = v[p1 + 4];
+		c[p1][2] = v[p1 + 8];
+		c[p1][3] = v[p1 + 12];
+		dft4(c[p1][0], c[p1][1], c[p1][2], c[p1][3]);
+	}
+	/* twiddles w16^{p1 k2}: p1 = 1: k2=1 w, 2 w^2, 3 w^3;
+	 * p1 = 2: w^2, w^4 = -j, w^6; p1 = 3: w^3, w^6, w^9 */
+	const float2 w1 = make_float2(FGK_COS_PI8, -FGK_SIN_PI8);
+	const float2 w3 = make_float2(FGK_SIN_PI8, -FGK_COS_PI8);
+	c[1][1] = cmul(c[1][1], w1);
+	c[1][2] = make_float2(FGK_SQRT1_2 * (c[1][2].x + c[1][2].y), FGK_SQRT1_2 * (c[1][2].y - c[1][2].x));
+	c[1][3] = cmul(c[1][3], w3);
+	c[2][1] = make_float2(FGK_SQRT1_2 * (c[2][1].x + c[2][1].y), FGK_SQRT1_2 * (c[2][1].y - c[2][1].x));
+	c[2][2] = mul_mj(c[2][2]);
+	c[2][3] = make_float2(FGK_SQRT1_2 * (c[2][3].y - c[2][3].x), -FGK_SQRT1_2 * (c[2][3].x + c[2][3].y));
+	c[3][1] = cmul(c[3][1], w3);
+	c[3][2] = make_float2(FGK_SQRT1_2 * (c[3][2].y - c[3][2].x), -FGK_SQRT1_2 * (c[3][2].x + c[3][2].y));
+	/* w16^9 = -w16^1 */
+	c[3][3] = cmul(c[3][3], make_float2(-FGK_COS_PI8, FGK_SIN_PI8));
+#pragma unroll
+	for (int k2 = 0; k2 < 4; k2++) {
+		dft4(c[0][k2], c[1][k2], c[2][k2], c[3][k2]);
+		v[k2] = c[0][k2];
+		v[k2 + 4] = c[1][k2];
+		v[k2 + 8] = c[2][k2];
+		v[k2 + 12] = c[3][k2];
+	}
+}
+
+template <int R> struct Radix;
+template <> struct Radix<2> { static FGK_HD void run(float2 *v) { dft2(v[0], v[1]); } };
+template <> struct Radix<3> { static FGK_HD void run(float2 *v) { dft3(v[0], v[1], v[2]); } };
+template <> struct Radix<4> { static FGK_HD void run(float2 *v) { dft4(v[0], v[1], v[2], v[3]); } };
+template <> struct Radix<5> { static FGK_HD void run(float2 *v) { dft5(v[0], v[1], v[2], v[3], v[4]); } };
+template <> struct Radix<8> { static FGK_HD void run(float2 *v) { dft8(v); } };
+template <> struct Radix<16> { static FGK_HD void run(float2 *v) { dft16(v); } };
+
+/* Good-Thomas prime-factor composite for N = A*B, gcd(A,B) = 1:
+ * input  n = (B n1 + A n2) mod N,
+ * output k = (B (B^-1 mod A) k1 + A (A^-1 mod B) k2) mod N. */
+constexpr int fgk_inv_mod(int a, int m, int t = 1)
+{
+	return ((a * t) % m == 1) ? t : fgk_inv_mod(a, m, t + 1);
+}
+
+template <int A, int B> struct PFA {
+	static FGK_HD void run(float2 *v)
+	{
+		constexpr int N = A * B;
+		float2 y[A][B];
+#pragma unroll
+		for (int n2 = 0; n2 < B; n2++) {
+			float2 col[A];
+#pragma unroll
+			for (int n1 = 0; n1 < A; n1++)
+				col[n1] = v[(B * n1 + A * n2) % N];
+			Radix<A>::run(col);
+#pragma unroll
+			for (int k1 = 0; k1 < A; k1++)
+				y[k1][n2] = col[k1];
+		}
+		constexpr int eA = (B * fgk_inv_mod(B % A, A)) % N;
+		constexpr int eB = (A * fgk_inv_mod(A % B, B)) % N;
+#pragma unroll
+		for (int k1 = 0; k1 < A; k1++) {
+			float2 row[B];
+#pragma unroll
+			for (int k2 = 0; k2 < B; k2++)
+				row[k2] = y[k1][k2];
+			Radix<B>::run(row);
+#pragma unroll
+			for (int k2 = 0; k2 < B; k2++)
+				v[(eA * k1 + eB * k2) % N] = row[k2];
+		}
+	}
+};
+template <> struct Radix<6> { static FGK_HD void run(float2 *v) { PFA<2, 3>::run(v); } };
+template <> struct Radix<10> { static FGK_HD void run(float2 *v) { PFA<2, 5>::run(v); } };
+template <> struct Radix<12> { static FGK_HD void run(float2 *v) { PFA<4, 3>::run(v); } };
+template <> struct Radix<15> { static FGK_HD void run(float2 *v) { PFA<3, 5>::run(v); } };
+
+} /* namespace fgk */

@@ -1,0 +1,154 @@
+/* fftset C API on GB300 (sm_103a).
+ *
+ * Drop-in for the reference library's public header (fftset.h of
+ * templeblock/fftset): same function names, argument order and meaning,
+ * buffer layouts and error behaviour, with C linkage. Each declaration cites
+ * the reference declaration it replaces. Entry points after "Additions" have
+ * no reference counterpart.
+ *
+ * Buffers may be device, managed or host memory. Device and managed buffers
+ * are used in place on the fftset's CUDA stream; host buffers are staged
+ * through device memory. Calls block until their results are in the output
+ * buffer, like the reference's CPU calls, unless fftset_set_blocking(fc, 0)
+ * is used (device buffers only; completion is then ordered on the stream). */
+#ifndef FFTSET_H
+#define FFTSET_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct fftset;             /* defined below so it can be placed on the stack (fftset.h:28-31) */
+struct fftset_modulation;  /* opaque (fftset.h:33-35) */
+struct fftset_fft;         /* opaque (fftset.h:37-39) */
+
+/* Initialization and Cleanup
+ * ------------------------------------------------------------------------ */
+
+/* replaces fftset.h:44-47 (src/fftset.c:80-85): returns zero on success,
+ * non-zero when memory (host or device) is exhausted or no CUDA device is
+ * usable. */
+int fftset_init(struct fftset *fc);
+
+/* replaces fftset.h:49-52 (src/fftset.c:87-95): frees every plan, twiddle
+ * table and staging buffer; all fftset_fft objects of fc become invalid. */
+void fftset_destroy(struct fftset *fc);
+
+/* Modulator Construction
+ * ------------------------------------------------------------------------ */
+
+/* replaces fftset.h:62-73: X[k] = sum_{n<N} x[n] e^{-j 2 pi n (k + 1/2) / N},
+ * x real, N = 2 complex_bins reals in, complex_bins interleaved bins out. */
+extern const struct fftset_modulation *FFTSET_MODULATION_FREQ_OFFSET_REAL;
+
+/* replaces fftset.h:75-76: the plain complex DFT of complex_bins points. */
+extern const struct fftset_modulation *FFTSET_MODULATION_COMPLEX;
+
+/* replaces fftset.h:78 (src/fftset.c:97-129): finds or creates the plan for
+ * (modulation, complex_bins); repeated calls return the same pointer.
+ * complex_bins must be 2^a 3^b 5^c with c <= 1 and complex_bins >= 2 (the
+ * sizes the reference supports, README.md:3); other sizes return NULL (the
+ * reference's behaviour for them is undefined), as does memory exhaustion.
+ * Not thread-safe, like the reference. */
+const struct fftset_fft *fftset_create_fft(struct fftset *fc, const struct fftset_modulation *modulation,
+                                           unsigned complex_bins);
+
+/* Modulator Execution
+ * ------------------------------------------------------------------------
+ * All buffers hold 2*complex_bins floats and must be 8-byte aligned (the
+ * reference asks for vector alignment, fftset.h:92-94). Aliasing rules are
+ * the reference's (fftset.h:93-96, :103-108). work_buf is accepted for
+ * compatibility; its contents are undefined after the call. */
+
+/* replaces fftset.h:109-115 (src/fftset.c:58-67) */
+void fftset_fft_forward(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf,
+                        float *work_buf);
+
+/* replaces fftset.h:117-123 (src/fftset.c:69-78): unnormalised,
+ * inverse(forward(x)) = complex_bins * x. */
+void fftset_fft_inverse(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf,
+                        float *work_buf);
+
+/* replaces fftset.h:125-130 (src/fftset.c:36-44). The output uses the
+ * reference's kernel-buffer layout for the SIMD width selected with
+ * fftset_set_kernel_layout (default 4), so kernels prepared here and by a CPU
+ * build of the reference are interchangeable. */
+void fftset_fft_conv_get_kernel(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf);
+
+/* replaces fftset.h:132-139 (src/fftset.c:46-56): FREQ_OFFSET_REAL gives
+ * complex_bins times the negacyclic convolution of length 2 complex_bins;
+ * COMPLEX gives complex_bins times the cyclic convolution. */
+void fftset_fft_conv(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf,
+                     const float *kernel_buf, float *work_buf);
+
+/* Helpful Routines
+ * ------------------------------------------------------------------------ */
+
+/* replaces fftset.h:144-151 (src/fftset.c:131-167), same result. */
+unsigned fftset_recommend_conv_length(unsigned kernel_length, unsigned max_block_size);
+
+/* Additions (no reference counterpart)
+ * ------------------------------------------------------------------------ */
+
+/* Error codes. Execution calls return void like the reference; a failure
+ * (bad argument, CUDA error) is latched in the fftset and read here. */
+#define FFTSET_OK               0
+#define FFTSET_E_INVALID        1  /* bad argument or size */
+#define FFTSET_E_NOMEM          2  /* host or device allocation failed */
+#define FFTSET_E_CUDA           3  /* a CUDA call failed; see fftset_cuda_error */
+#define FFTSET_E_UNSUPPORTED    4  /* plan cannot run this operation */
+int         fftset_last_error(const struct fftset *fc);      /* returns and keeps the latched code */
+int         fftset_clear_error(struct fftset *fc);           /* returns the code and resets it */
+int         fftset_cuda_error(const struct fftset *fc);      /* cudaError_t of the last CUDA failure */
+const char *fftset_error_string(int code);
+
+/* CUDA stream (a cudaStream_t) every call of fc is ordered on; NULL = the
+ * stream fftset_init created. */
+int  fftset_set_stream(struct fftset *fc, void *cuda_stream);
+void *fftset_get_stream(const struct fftset *fc);
+/* 1 (default): calls return after their results are in place. 0: calls
+ * with device buffers only enqueue work on the stream. */
+int  fftset_set_blocking(struct fftset *fc, int blocking);
+/* Kernel-buffer layout of fftset_fft_conv_get_kernel / fftset_fft_conv:
+ * that of a reference build with SIMD width 1, 4 (default) or 8. Applies to
+ * plans created afterwards. */
+int  fftset_set_kernel_layout(struct fftset *fc, unsigned simd_width);
+/* Kernel-buffer layout without a GPU: re_offsets[bin] (complex_bins
+ * entries) receives the float offset of the real part of DFT bin `bin` in
+ * the buffer fftset_fft_conv_get_kernel writes for a reference build of SIMD
+ * width simd_width; the imaginary part is at re_offsets[bin] + *lanes. */
+int fftset_kernel_layout(const struct fftset_modulation *modulation, unsigned complex_bins, unsigned simd_width,
+                         int *re_offsets, unsigned *lanes);
+/* Lane width of the kernel-buffer layout of one plan (1, 4 or 8). */
+unsigned fftset_fft_kernel_lanes(const struct fftset_fft *fft);
+unsigned fftset_fft_bins(const struct fftset_fft *fft);
+
+/* Batched forms of the four execution calls: `count` independent blocks,
+ * block b at input_buf + b*in_stride and output_buf + b*out_stride floats
+ * (strides >= 2*complex_bins). One launch for all blocks. Return an error
+ * code (also latched). Aliasing: as for the single-block calls, block by
+ * block. */
+int fftset_fft_forward_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
+                             const float *input_buf, size_t in_stride, unsigned count);
+int fftset_fft_inverse_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
+                             const float *input_buf, size_t in_stride, unsigned count);
+int fftset_fft_conv_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
+                          const float *input_buf, size_t in_stride, const float *kernel_buf, unsigned count);
+int fftset_fft_conv_get_kernel_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
+                                     const float *input_buf, size_t in_stride, unsigned count);
+
+/* Private Parts
+ * ---------------------------------------------------------------------------
+ * Don't touch them. */
+struct fftset {
+	void *impl;
+	void *reserved[7];
+};
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFTSET_H */

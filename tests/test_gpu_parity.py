@@ -1,0 +1,272 @@
+"""GPU parity through the C ABI: every execution call against the unmodified
+reference's outputs (tests/golden), the FP64 oracle, the reference's own
+known-answer tests, and the edge cases of its contract (aliasing, odd sizes,
+unsupported sizes, host buffers, batched calls). Tolerance: relative L2 <=
+2e-6 * log2(N), N the transform length in reals (FREQ_OFFSET_REAL: 2L) or
+complex points (COMPLEX: L)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(m, L) for m in (0, 1) for L in O.REFERENCE_TEST_LENGTHS] + [(0, 1024), (1, 1536), (1, 4096)]
+
+
+def tol(mod, L):
+    return O.tolerance(2 * L if mod else L)
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def _g(golden, mod, L, what):
+    return golden[f"m{mod}_L{L}_{what}"]
+
+
+@pytest.mark.parametrize("mod,L", CASES)
+def test_forward_matches_reference(gpu_set, golden_outputs, mod, L):
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    x = _g(golden_outputs, mod, L, "x")
+    out = torch.empty(2 * L, device="cuda")
+    f.forward(out, dev(x))
+    y = host(out)
+    assert O.rel_l2(y, _g(golden_outputs, mod, L, "fwd")) <= tol(mod, L)
+    assert O.rel_l2(y, O.forward64(mod, x)) <= tol(mod, L)
+
+
+@pytest.mark.parametrize("mod,L", CASES)
+def test_inverse_matches_reference(gpu_set, golden_outputs, mod, L):
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    X = _g(golden_outputs, mod, L, "fwd")
+    out = torch.empty(2 * L, device="cuda")
+    f.inverse(out, dev(X))
+    y = host(out)
+    assert O.rel_l2(y, _g(golden_outputs, mod, L, "inv")) <= tol(mod, L)
+    assert O.rel_l2(y, O.inverse64(mod, X)) <= tol(mod, L)
+    # in place, as the reference's own test calls it (fftset_test.c:142)
+    buf = dev(X)
+    f.inverse(buf, buf)
+    assert O.rel_l2(host(buf), y) <= 1e-7
+
+
+@pytest.mark.parametrize("mod,L", CASES)
+def test_get_kernel_matches_reference_layout(gpu_set, golden_outputs, mod, L):
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    h = _g(golden_outputs, mod, L, "h")
+    out = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(out, dev(h))
+    assert O.rel_l2(host(out), _g(golden_outputs, mod, L, "kern")) <= tol(mod, L)
+
+
+@pytest.mark.parametrize("mod,L", CASES)
+def test_conv_matches_reference(gpu_set, golden_outputs, mod, L):
+    """conv with the kernel buffer the REFERENCE prepared (layout interop),
+    and with our own; in place (input_buf == output_buf) as the reference
+    allows and its test does (fftset_test.c:198)."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    x = _g(golden_outputs, mod, L, "x")
+    Kref = _g(golden_outputs, mod, L, "kern")
+    want = _g(golden_outputs, mod, L, "conv")
+    out = torch.empty(2 * L, device="cuda")
+    f.conv(out, dev(x), dev(Kref))
+    assert O.rel_l2(host(out), want) <= tol(mod, L)
+    assert O.rel_l2(host(out), O.conv64(mod, x, _g(golden_outputs, mod, L, "h"))) <= tol(mod, L)
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(_g(golden_outputs, mod, L, "h")))
+    buf = dev(x)
+    f.conv(buf, buf, K)
+    assert O.rel_l2(host(buf), want) <= tol(mod, L)
+
+
+@pytest.mark.parametrize("L", O.REFERENCE_TEST_LENGTHS)
+def test_reference_kats_on_gpu(gpu_set, L):
+    """The reference's own known-answer tests (app_fftset_test/fftset_test.c)
+    with its RMS thresholds, through the C ABI."""
+    import torch
+    N = 2 * L
+    flags = O.prime_flags(N)
+    # FREQ_OFFSET_REAL prime impulse (:70-156)
+    f = gpu_set.create_fft(1, L)
+    x = flags.astype(np.float32)
+    X = torch.empty(N, device="cuda")
+    f.forward(X, dev(x))
+    Xh = host(X).astype(np.float64)
+    err = Xh - O.freqoff_direct64(x)
+    assert np.sqrt((err[0::2] ** 2 + err[1::2] ** 2).sum() / L) <= 4e-6
+    f.inverse(X, X)
+    r = host(X) / L - x
+    assert np.sqrt((r ** 2).sum() / L) <= 1e-6
+    # convolution (:158-222)
+    h = np.where(flags & (np.arange(N) < N // 4), 2.0 / N, 0.0).astype(np.float32)
+    s = np.where(flags & (np.arange(N) < 3 * N // 4), 1.0, 0.0).astype(np.float32)
+    K = torch.empty(N, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    y = dev(s)
+    f.conv(y, y, K)
+    exp = np.zeros(N)
+    for a in np.nonzero(s)[0]:
+        for b in np.nonzero(h)[0]:
+            exp[a + b] += 1.0
+    assert np.sqrt(((exp - host(y)) ** 2).sum() / L) <= 1e-5
+    # COMPLEX prime impulse (:224-314), inverse checked on all 2L floats
+    g = gpu_set.create_fft(0, L)
+    Xc = torch.empty(N, device="cuda")
+    g.forward(Xc, dev(x))
+    err = host(Xc).astype(np.float64) - O.complex_forward64(x)
+    assert np.sqrt((err[0::2] ** 2 + err[1::2] ** 2).sum() / L) <= 4e-6
+    g.inverse(Xc, Xc)
+    r = host(Xc) / L - x
+    assert np.sqrt((r ** 2).sum() / L) <= 1e-6
+
+
+def _all_sizes():
+    return O.valid_sizes(2, 4096)
+
+
+@pytest.mark.parametrize("mod", [0, 1])
+def test_every_size_to_4096_against_fp64(gpu_set, mod):
+    """Every supported size 2..4096: forward, inverse, conv vs FP64."""
+    import torch
+    rng = np.random.default_rng(11 + mod)
+    for L in _all_sizes():
+        f = gpu_set.create_fft(mod, L)
+        assert f is not None, L
+        x = rng.standard_normal(2 * L).astype(np.float32)
+        h = rng.standard_normal(2 * L).astype(np.float32)
+        X = torch.empty(2 * L, device="cuda")
+        f.forward(X, dev(x))
+        Xh = host(X)
+        assert O.rel_l2(Xh, O.forward64(mod, x)) <= tol(mod, L), L
+        r = torch.empty(2 * L, device="cuda")
+        f.inverse(r, X)
+        assert O.rel_l2(host(r), O.inverse64(mod, Xh)) <= tol(mod, L), L
+        K = torch.empty(2 * L, device="cuda")
+        f.conv_get_kernel(K, dev(h))
+        y = torch.empty(2 * L, device="cuda")
+        f.conv(y, dev(x), K)
+        assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L), L
+
+
+@pytest.mark.parametrize("mod,L", [(0, 8192), (1, 8192), (0, 12288), (1, 15360), (0, 16384), (1, 16384),
+                                   (1, 20736), (0, 25920), (1, 26244)])
+def test_large_resident_sizes_against_fp64(gpu_set, mod, L):
+    import torch
+    rng = np.random.default_rng(L)
+    f = gpu_set.create_fft(mod, L)
+    assert f is not None
+    x = rng.standard_normal((3, 2 * L)).astype(np.float32)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    X = torch.empty(3, 2 * L, device="cuda")
+    f.forward_batch(X, dev(x))
+    Xh = host(X)
+    assert O.rel_l2(Xh, O.forward64(mod, x)) <= tol(mod, L)
+    r = torch.empty_like(X)
+    f.inverse_batch(r, X)
+    assert O.rel_l2(host(r), O.inverse64(mod, Xh)) <= tol(mod, L)
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    y = torch.empty_like(X)
+    f.conv_batch(y, dev(x), K)
+    assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
+
+
+@pytest.mark.parametrize("mod,L", [(1, 1536), (0, 1024), (1, 45), (0, 27), (1, 4096), (0, 60)])
+def test_batch_equals_single_calls(gpu_set, mod, L):
+    """Batched entry points with padded strides give the single-call result
+    block by block, and leave the padding untouched."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    rng = np.random.default_rng(3)
+    B, pad = 37, 6
+    x = rng.standard_normal((B, 2 * L + pad)).astype(np.float32)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    xd = dev(x)
+    for op in ("forward", "inverse", "conv"):
+        out = torch.full((B, 2 * L + pad), 7.0, device="cuda")
+        if op == "conv":
+            f.conv_batch(out, xd, K)
+        else:
+            getattr(f, op + "_batch")(out, xd)
+        ob = host(out)
+        assert np.all(ob[:, 2 * L:] == 7.0)
+        for b in (0, 1, B // 2, B - 1):
+            single = torch.empty(2 * L, device="cuda")
+            src = dev(x[b, :2 * L])
+            if op == "conv":
+                f.conv(single, src, K)
+            else:
+                getattr(f, op)(single, src)
+            assert np.array_equal(host(single), ob[b, :2 * L]), (op, b)
+
+
+def test_host_buffers_are_staged(gpu_set, golden_outputs):
+    """numpy (host) buffers go through the staging path and give the same
+    results as device buffers."""
+    mod, L = 1, 1536
+    f = gpu_set.create_fft(mod, L)
+    x = _g(golden_outputs, mod, L, "x").copy()
+    K = _g(golden_outputs, mod, L, "kern").copy()
+    y = np.empty_like(x)
+    f.conv(y, x, K)
+    assert O.rel_l2(y, _g(golden_outputs, mod, L, "conv")) <= tol(mod, L)
+    X = np.empty_like(x)
+    f.forward(X, x)
+    assert O.rel_l2(X, _g(golden_outputs, mod, L, "fwd")) <= tol(mod, L)
+    f.inverse(X, X)
+    assert O.rel_l2(X, O.inverse64(mod, _g(golden_outputs, mod, L, "fwd"))) <= tol(mod, L)
+
+
+def test_unsupported_sizes_return_null(gpu_set):
+    for L in (0, 1, 7, 25, 49, 3 * 7 * 16, 50):
+        assert gpu_set.create_fft(1, L) is None
+        assert gpu_set.create_fft(0, L) is None
+
+
+def test_plans_are_shared(gpu_set):
+    a = gpu_set.create_fft(1, 1536)
+    b = gpu_set.create_fft(1, 1536)
+    c = gpu_set.create_fft(0, 1536)
+    assert a.handle == b.handle and a.handle != c.handle
+
+
+@pytest.mark.parametrize("vw", [1, 8])
+def test_other_simd_layouts(fftset_lib, golden_layouts, vw):
+    """Kernel buffers in the layout of width-1 and width-8 reference builds."""
+    import torch
+    S = fftset_lib.FftSet(kernel_layout_width=vw)
+    rng = np.random.default_rng(vw)
+    try:
+        for mod, L in ((1, 1536), (1, 576), (0, 1024), (1, 96), (0, 45)):
+            f = S.create_fft(mod, L)
+            h = rng.standard_normal(2 * L).astype(np.float32)
+            K = torch.empty(2 * L, device="cuda")
+            f.conv_get_kernel(K, dev(h))
+            off = golden_layouts[f"vw{vw}_m{mod}_L{L}"].astype(np.int64)
+            V = f.kernel_lanes
+            W = O.spectrum64(mod, h)
+            want = np.zeros(2 * L)
+            want[off] = W.real
+            want[off + V] = W.imag
+            assert O.rel_l2(host(K), want) <= tol(mod, L)
+            x = rng.standard_normal(2 * L).astype(np.float32)
+            y = torch.empty(2 * L, device="cuda")
+            f.conv(y, dev(x), K)
+            assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
+    finally:
+        S.close()
