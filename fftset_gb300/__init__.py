@@ -56,6 +56,7 @@ _decl("fftset_cuda_error", C.c_int, [_P])
 _decl("fftset_error_string", C.c_char_p, [C.c_int])
 _decl("fftset_set_stream", C.c_int, [_P, _vp])
 _decl("fftset_get_stream", _vp, [_P])
+_decl("fftset_own_stream", _vp, [_P])
 _decl("fftset_set_blocking", C.c_int, [_P, C.c_int])
 _decl("fftset_set_kernel_layout", C.c_int, [_P, _u])
 _decl("fftset_kernel_layout", C.c_int, [_vp, _u, _u, C.POINTER(C.c_int), C.POINTER(_u)])
@@ -64,6 +65,12 @@ _decl("fftset_fft_bins", _u, [_vp])
 for _n in ("fftset_fft_forward_batch", "fftset_fft_inverse_batch", "fftset_fft_conv_get_kernel_batch"):
     _decl(_n, C.c_int, [_vp, _vp, _sz, _vp, _sz, _u])
 _decl("fftset_fft_conv_batch", C.c_int, [_vp, _vp, _sz, _vp, _sz, _vp, _u])
+_decl("fftset_fft_variants", C.c_int, [_vp])
+_decl("fftset_fft_variant", C.c_int, [_vp, C.c_int])
+_decl("fftset_fft_set_variant", C.c_int, [_vp, C.c_int, C.c_int])
+_decl("fftset_fft_autotune", C.c_int, [_vp, C.c_int, _u, C.POINTER(C.c_float)])
+
+OP_FORWARD, OP_INVERSE, OP_GET_KERNEL, OP_CONV, OP_CORR = range(5)
 
 MODULATION_COMPLEX = _vp.in_dll(_lib, "FFTSET_MODULATION_COMPLEX").value
 MODULATION_FREQ_OFFSET_REAL = _vp.in_dll(_lib, "FFTSET_MODULATION_FREQ_OFFSET_REAL").value
@@ -159,9 +166,13 @@ class FftSet:
             raise FftsetError(error_string(rc))
 
     def set_stream(self, stream):
-        """stream: a torch.cuda.Stream, an int cudaStream_t, or None."""
+        """stream: a torch.cuda.Stream or an int cudaStream_t (0 = CUDA's
+        legacy default stream)."""
         s = getattr(stream, "cuda_stream", stream)
-        _lib.fftset_set_stream(C.byref(self._s), s)
+        _lib.fftset_set_stream(C.byref(self._s), s if s else None)
+
+    def own_stream(self):
+        return _lib.fftset_own_stream(C.byref(self._s))
 
     def set_blocking(self, blocking: bool):
         _lib.fftset_set_blocking(C.byref(self._s), 1 if blocking else 0)
@@ -194,6 +205,30 @@ class Fft:
         self.handle = handle
         self.bins = int(_lib.fftset_fft_bins(handle))
         self.kernel_lanes = int(_lib.fftset_fft_kernel_lanes(handle))
+
+    @property
+    def variants(self) -> int:
+        return int(_lib.fftset_fft_variants(self.handle))
+
+    def variant(self, op: int) -> int:
+        return int(_lib.fftset_fft_variant(self.handle, op))
+
+    def set_variant(self, op: int, variant: int):
+        rc = _lib.fftset_fft_set_variant(self.handle, op, variant)
+        if rc:
+            raise FftsetError(error_string(rc))
+
+    def autotune(self, op: int, count: int) -> float:
+        """Time every kernel for `op` on `count` blocks; keep the fastest.
+        Returns its time in ms."""
+        import torch
+        self.owner.set_stream(torch.cuda.current_stream())
+        ms = C.c_float(0)
+        rc = _lib.fftset_fft_autotune(self.handle, op, count, C.byref(ms))
+        if rc:
+            self.owner.check()
+            raise FftsetError(error_string(rc))
+        return float(ms.value)
 
     def _sync_stream(self, *bufs):
         if _is_cuda(*bufs):

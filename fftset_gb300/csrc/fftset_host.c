@@ -38,13 +38,19 @@ const struct fftset_modulation *FFTSET_MODULATION_COMPLEX = &FS_MOD_COMPLEX;
 
 struct fs_impl;
 
+#define FS_MAX_VAR 8
+
 struct fftset_fft {
 	unsigned                        lfft;
 	const struct fftset_modulation *modulator;
 	struct fftset_fft              *next;
 	struct fs_impl                 *fs;
 	unsigned                        lanes; /* kernel-buffer lane width */
-	fgk_plan                        rp;    /* resident plan (device pointers inside) */
+	fgk_plan                        rp;    /* generic resident plan (device pointers inside) */
+	int                             nvar;  /* compile-time kernel variants for this size */
+	fgk_plan                        vp[FS_MAX_VAR]; /* their plans (chain of the variant) */
+	uint32_t                        vops[FS_MAX_VAR]; /* ops each variant implements (1 << op) */
+	int                             sel[FGK_OP_COUNT]; /* chosen variant per op, -1 = generic */
 	void                           *dmem;  /* one device block for all tables */
 };
 
@@ -59,6 +65,7 @@ struct fs_impl {
 	int                cuda_err;
 	int                device;
 	unsigned           max_smem;
+	int                num_sms;
 	struct fftset_fft *first;
 	pthread_mutex_t    lock;
 	void              *stage[FS_NSTAGE];
@@ -91,7 +98,7 @@ static int fs_cuda(struct fs_impl *fs, cudaError_t e)
 int fftset_init(struct fftset *fc)
 {
 	struct fs_impl *fs;
-	int dev = 0, smem = 0;
+	int dev = 0, smem = 0, sms = 0;
 	if (fc == NULL)
 		return -1;
 	memset(fc, 0, sizeof(*fc));
@@ -99,7 +106,8 @@ int fftset_init(struct fftset *fc)
 		cudaGetLastError();
 		return -1;
 	}
-	if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+	if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+	    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
 		cudaGetLastError();
 		return -1;
 	}
@@ -121,6 +129,7 @@ int fftset_init(struct fftset *fc)
 	fs->layout_vw = 4;
 	fs->device = dev;
 	fs->max_smem = (unsigned)smem;
+	fs->num_sms = sms;
 	fc->impl = fs;
 	return 0;
 }
@@ -167,27 +176,51 @@ static size_t fs_align(size_t x)
 	return (x + 255) & ~(size_t)255;
 }
 
-/* Build the device tables of a resident plan. */
+/* Build the device tables of a plan: the generic resident plan (chain from
+ * the GPU planner) plus one twiddle table per compile-time variant (each
+ * variant has its own chain); modulation factors and the kernel-layout index
+ * table are shared. Everything lives in one device allocation. */
 static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 {
 	fgk_plan *rp = &f->rp;
-	size_t ntw, o_plan, o_tw, o_mod, o_kidx, total;
+	size_t ntw, vtw[FS_MAX_VAR], o_plan, o_tw, o_mod, o_kidx, o_v[FS_MAX_VAR], total;
 	float *tw = NULL, *mod = NULL;
 	int32_t *kidx = NULL;
 	char *d = NULL;
 	unsigned L = f->lfft, i, lanes = 0;
-	int rc = FFTSET_E_NOMEM;
+	uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
+	int rc = FFTSET_E_NOMEM, v, op, nvar;
 	cudaError_t e;
 
-	if (fgk_plan_resident(rp, L, f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX, fs->max_smem))
+	if (fgk_plan_resident(rp, L, modulation, fs->max_smem, NULL, 0))
 		return FFTSET_E_UNSUPPORTED;
 	ntw = fgk_plan_twiddles(rp, NULL);
-	tw = (float *)malloc(sizeof(float) * 2 * (ntw ? ntw : 1));
+	nvar = fgk_static_count(modulation, L);
+	if (nvar > FS_MAX_VAR)
+		nvar = FS_MAX_VAR;
+	f->nvar = 0;
+	for (v = 0; v < nvar; v++) {
+		uint32_t rad[FGK_MAX_STAGES], n, threads, groups, ops;
+		if (!fgk_static_info(modulation, L, v, rad, &n, &threads, &groups, &ops) ||
+		    fgk_plan_resident(&f->vp[v], L, modulation, fs->max_smem, rad, n))
+			return FFTSET_E_UNSUPPORTED;
+		f->vops[v] = ops;
+		vtw[v] = fgk_plan_twiddles(&f->vp[v], NULL);
+	}
+	f->nvar = nvar;
+	for (op = 0; op < FGK_OP_COUNT; op++) {
+		f->sel[op] = -1;
+		for (v = 0; v < nvar; v++)
+			if (f->vops[v] & (1u << op)) {
+				f->sel[op] = v;
+				break;
+			}
+	}
+
 	mod = (float *)malloc(sizeof(float) * 2 * L);
 	kidx = (int32_t *)malloc(sizeof(int32_t) * L);
-	if (!tw || !mod || !kidx)
+	if (!mod || !kidx)
 		goto out;
-	fgk_plan_twiddles(rp, tw);
 	for (i = 0; i < L; i++) {
 		double a = -M_PI * (double)i / (2.0 * (double)L);
 		mod[2 * i + 0] = (float)cos(a);
@@ -205,6 +238,10 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 	o_mod = o_tw + fs_align(sizeof(float) * 2 * (ntw ? ntw : 1));
 	o_kidx = o_mod + fs_align(sizeof(float) * 2 * L);
 	total = o_kidx + fs_align(sizeof(int32_t) * L);
+	for (v = 0; v < nvar; v++) {
+		o_v[v] = total;
+		total += fs_align(sizeof(float) * 2 * (vtw[v] ? vtw[v] : 1));
+	}
 	e = cudaMalloc((void **)&d, total);
 	if (e != cudaSuccess) {
 		cudaGetLastError();
@@ -214,17 +251,40 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 	rp->modtw = d + o_mod;
 	rp->kidx = (const int32_t *)(d + o_kidx);
 	rp->dev = (const fgk_plan *)(d + o_plan);
-	if ((e = cudaMemcpy(d + o_tw, tw, sizeof(float) * 2 * ntw, cudaMemcpyHostToDevice)) != cudaSuccess ||
-	    (e = cudaMemcpy(d + o_mod, mod, sizeof(float) * 2 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	if ((e = cudaMemcpy(d + o_mod, mod, sizeof(float) * 2 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
 	    (e = cudaMemcpy(d + o_kidx, kidx, sizeof(int32_t) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
-	    (e = cudaMemcpy(d + o_plan, rp, sizeof(fgk_plan), cudaMemcpyHostToDevice)) != cudaSuccess) {
-		fs_cuda(fs, e);
-		cudaFree(d);
-		rc = FFTSET_E_CUDA;
-		goto out;
+	    (e = cudaMemcpy(d + o_plan, rp, sizeof(fgk_plan), cudaMemcpyHostToDevice)) != cudaSuccess)
+		goto cuda_fail;
+	/* twiddle tables, one host buffer at a time */
+	for (v = -1; v < nvar; v++) {
+		fgk_plan *pp = v < 0 ? rp : &f->vp[v];
+		size_t nt = v < 0 ? ntw : vtw[v];
+		tw = (float *)malloc(sizeof(float) * 2 * (nt ? nt : 1));
+		if (!tw) {
+			cudaFree(d);
+			goto out;
+		}
+		fgk_plan_twiddles(pp, tw);
+		if (v >= 0) {
+			pp->tw = d + o_v[v];
+			pp->modtw = rp->modtw;
+			pp->kidx = rp->kidx;
+			pp->kvw = lanes;
+			pp->dev = NULL;
+		}
+		e = cudaMemcpy((void *)pp->tw, tw, sizeof(float) * 2 * nt, cudaMemcpyHostToDevice);
+		free(tw);
+		tw = NULL;
+		if (e != cudaSuccess)
+			goto cuda_fail;
 	}
 	f->dmem = d;
 	rc = FFTSET_OK;
+	goto out;
+cuda_fail:
+	fs_cuda(fs, e);
+	cudaFree(d);
+	rc = FFTSET_E_CUDA;
 out:
 	free(tw);
 	free(mod);
@@ -312,6 +372,31 @@ static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 	return FFTSET_OK;
 }
 
+/* Kernel choice: the compile-time kernel when one exists and the batch is
+ * large enough to amortise its per-CTA table staging; the generic resident
+ * kernel otherwise. */
+#define FS_STATIC_MIN_COUNT 64
+
+static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *out, const float *in,
+                             const float *kern, unsigned count, size_t in_stride, size_t out_stride)
+{
+	struct fs_impl *fs = f->fs;
+	if (v >= 0 && v < f->nvar) {
+		int rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, fs->stream,
+		                           fs->num_sms);
+		if (rc >= 0)
+			return rc;
+	}
+	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
+}
+
+static int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
+                     unsigned count, size_t in_stride, size_t out_stride)
+{
+	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
+	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride);
+}
+
 /* Runs op on `count` blocks. Buffers of any memory kind. */
 static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in,
                    size_t in_stride, const float *kern, unsigned count)
@@ -332,13 +417,16 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		return fs_latch(fs, FFTSET_E_INVALID, 0);
 	if ((((uintptr_t)in) | ((uintptr_t)out) | ((uintptr_t)kern)) & 7)
 		return fs_latch(fs, FFTSET_E_INVALID, 0);
+	/* blocks must stay 8-byte aligned (complex values are read as pairs) */
+	if (count > 1 && ((in_stride | out_stride) & 1))
+		return fs_latch(fs, FFTSET_E_INVALID, 0);
 	if (count == 0)
 		return FFTSET_OK;
 	in_span = (size_t)(count - 1) * in_stride + nf;
 	out_span = (size_t)(count - 1) * out_stride + nf;
 
 	if (fs_is_device_ptr(in) && fs_is_device_ptr(out) && (kern == NULL || fs_is_device_ptr(kern))) {
-		rc = fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
+		rc = fs_launch(f, op, out, in, kern, count, in_stride, out_stride);
 		if (rc)
 			return fs_latch(fs, FFTSET_E_CUDA, rc);
 		if (fs->blocking)
@@ -374,7 +462,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 			goto done;
 		dout = (float *)fs->stage[1];
 	}
-	rc = fgk_launch_resident(&f->rp, op, dout, din, dkern, count, in_stride, out_stride, fs->stream);
+	rc = fs_launch(f, op, dout, din, dkern, count, in_stride, out_stride);
 	if (rc) {
 		rc = fs_latch(fs, FFTSET_E_CUDA, rc);
 		goto done;
@@ -513,7 +601,7 @@ int fftset_set_stream(struct fftset *fc, void *cuda_stream)
 	struct fs_impl *fs = fs_of(fc);
 	if (!fs)
 		return FFTSET_E_INVALID;
-	fs->stream = cuda_stream ? (cudaStream_t)cuda_stream : fs->own_stream;
+	fs->stream = (cudaStream_t)cuda_stream;
 	return FFTSET_OK;
 }
 
@@ -521,6 +609,12 @@ void *fftset_get_stream(const struct fftset *fc)
 {
 	struct fs_impl *fs = fs_of(fc);
 	return fs ? (void *)fs->stream : NULL;
+}
+
+void *fftset_own_stream(const struct fftset *fc)
+{
+	struct fs_impl *fs = fs_of(fc);
+	return fs ? (void *)fs->own_stream : NULL;
 }
 
 int fftset_set_blocking(struct fftset *fc, int blocking)
@@ -561,4 +655,101 @@ int fftset_kernel_layout(const struct fftset_modulation *modulation, unsigned co
 	if (fsl_kernel_offsets(modulation->freq_offset_real, complex_bins, simd_width, (int32_t *)re_offsets, lanes))
 		return FFTSET_E_INVALID;
 	return FFTSET_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * Kernel variants and the autotuner */
+
+int fftset_fft_variants(const struct fftset_fft *fft)
+{
+	return fft ? fft->nvar : 0;
+}
+
+int fftset_fft_variant(const struct fftset_fft *fft, int op)
+{
+	if (!fft || op < 0 || op >= FGK_OP_COUNT)
+		return -1;
+	return fft->sel[op];
+}
+
+int fftset_fft_set_variant(const struct fftset_fft *fft, int op, int variant)
+{
+	struct fftset_fft *f = (struct fftset_fft *)fft; /* the plan object is the library's own */
+	if (!f || op < 0 || op >= FGK_OP_COUNT || variant < -1 || variant >= f->nvar)
+		return FFTSET_E_INVALID;
+	if (variant >= 0 && !(f->vops[variant] & (1u << op)))
+		return FFTSET_E_UNSUPPORTED;
+	f->sel[op] = variant;
+	return FFTSET_OK;
+}
+
+/* Times every kernel that can run `op` for this plan (the generic resident
+ * kernel and each compile-time variant) on `count` blocks of scratch device
+ * memory, and selects the fastest for batched calls of that op. */
+int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, float *best_ms)
+{
+	struct fftset_fft *f = (struct fftset_fft *)fft;
+	struct fs_impl *fs;
+	float *in = NULL, *out = NULL, *kern = NULL, best = -1.0f;
+	size_t nf;
+	cudaEvent_t e0 = NULL, e1 = NULL;
+	cudaError_t e;
+	int v, rep, bestv = -1, rc = FFTSET_OK;
+	if (!f || op < 0 || op >= FGK_OP_COUNT || count == 0)
+		return FFTSET_E_INVALID;
+	fs = f->fs;
+	nf = 2 * (size_t)f->lfft;
+	if ((e = cudaMalloc((void **)&in, nf * count * sizeof(float))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&out, nf * count * sizeof(float))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&kern, nf * sizeof(float))) != cudaSuccess) {
+		cudaGetLastError();
+		rc = fs_latch(fs, FFTSET_E_NOMEM, (int)e);
+		goto done;
+	}
+	if ((e = cudaMemsetAsync(in, 0, nf * count * sizeof(float), fs->stream)) != cudaSuccess ||
+	    (e = cudaMemsetAsync(kern, 0, nf * sizeof(float), fs->stream)) != cudaSuccess ||
+	    (e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess) {
+		rc = fs_cuda(fs, e);
+		goto done;
+	}
+	for (v = -1; v < f->nvar; v++) {
+		float ms = 0, vbest = -1.0f;
+		if (v >= 0 && !(f->vops[v] & (1u << op)))
+			continue;
+		for (rep = 0; rep < 7; rep++) {
+			if ((e = cudaEventRecord(e0, fs->stream)) != cudaSuccess) {
+				rc = fs_cuda(fs, e);
+				goto done;
+			}
+			if ((rc = fs_launch_variant(f, v, op, out, in, kern, count, nf, nf)) != 0) {
+				rc = fs_latch(fs, FFTSET_E_CUDA, rc);
+				goto done;
+			}
+			if ((e = cudaEventRecord(e1, fs->stream)) != cudaSuccess ||
+			    (e = cudaEventSynchronize(e1)) != cudaSuccess ||
+			    (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) {
+				rc = fs_cuda(fs, e);
+				goto done;
+			}
+			if (rep >= 2 && (vbest < 0 || ms < vbest))
+				vbest = ms;
+		}
+		if (best < 0 || vbest < best) {
+			best = vbest;
+			bestv = v;
+		}
+	}
+	f->sel[op] = bestv;
+	if (best_ms)
+		*best_ms = best;
+done:
+	if (e0)
+		cudaEventDestroy(e0);
+	if (e1)
+		cudaEventDestroy(e1);
+	cudaStreamSynchronize(fs->stream);
+	cudaFree(in);
+	cudaFree(out);
+	cudaFree(kern);
+	return rc;
 }

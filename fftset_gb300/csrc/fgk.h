@@ -61,7 +61,9 @@ typedef struct fgk_plan {
 
 /* Host-side planning helpers implemented in fgk_plan.c */
 int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
-int  fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes);
+/* forced_radices: NULL, or the chain a static kernel was compiled for */
+int  fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes,
+                       const uint32_t *forced_radices, uint32_t forced_n);
 /* Number of float2 twiddles both chains of p need; fills them when tw != NULL. */
 size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2);
 
@@ -69,6 +71,18 @@ size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2);
 int fgk_launch_resident(const fgk_plan *p, int op, float *out, const float *in, const float *kern,
                         uint32_t count, size_t in_stride, size_t out_stride, void *stream);
 uint32_t fgk_max_resident_L(void);
+
+/* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
+ * variants exist for (modulation, L); fgk_static_info describes variant v
+ * (chain, threads per transform, transforms per CTA, compiled ops as a bit
+ * mask of 1 << fgk_op). The plan passed to fgk_launch_static must have been
+ * made with that variant's chain. fgk_launch_static returns -1 when the
+ * variant does not implement op. */
+int fgk_static_count(uint32_t modulation, uint32_t L);
+int fgk_static_info(uint32_t modulation, uint32_t L, int v, uint32_t *radices, uint32_t *n, uint32_t *threads,
+                    uint32_t *groups, uint32_t *opmask);
+int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
+                      uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ static const struct {
 #define FGK_MAXE2 32
 #define FGK_MAXE3 21
 #define FGK_MAXE5 2
-static uint32_t best_chain(uint32_t a, uint32_t b, uint32_t c, uint32_t *chain, uint32_t *n)
+static uint32_t best_chain(uint32_t a, uint32_t b, uint32_t c, uint32_t allowed, uint32_t *chain, uint32_t *n)
 {
 	static uint32_t cost[FGK_MAXE2][FGK_MAXE3][FGK_MAXE5];
 	static uint8_t  first[FGK_MAXE2][FGK_MAXE3][FGK_MAXE5];
@@ -53,6 +53,8 @@ static uint32_t best_chain(uint32_t a, uint32_t b, uint32_t c, uint32_t *chain, 
 				}
 				for (i = 0; i < FGK_NRADIX; i++) {
 					uint32_t sc, tot;
+					if (!(allowed & (1u << i)))
+						continue;
 					if (FGK_RADIX[i].e2 > i2 || FGK_RADIX[i].e3 > i3 || FGK_RADIX[i].e5 > i5)
 						continue;
 					sc = cost[i2 - FGK_RADIX[i].e2][i3 - FGK_RADIX[i].e3][i5 - FGK_RADIX[i].e5];
@@ -97,12 +99,17 @@ static int factor235(uint32_t L, uint32_t *a, uint32_t *b, uint32_t *c)
 /* Chain of radices, largest first: then every stage after the first sees
  * ns >= 16 when the first radix is 16, which keeps the Stockham scatter free of
  * shared-memory bank conflicts under the i + i/16 padding. */
-int fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages)
+/* radix sets: all codelets, or only those whose register tile divides a
+ * 16/32-element budget well (used when the full set needs > 1024 threads) */
+#define FGK_ALL_RADICES 0x3ffu
+#define FGK_SMALL_RADICES ((1u << 0) | (1u << 4) | (1u << 6) | (1u << 7) | (1u << 8) | (1u << 9))
+
+static int plan_chain_set(uint32_t L, uint32_t allowed, uint32_t *radices, uint32_t *nstages)
 {
 	uint32_t a, b, c, i, j;
 	if (factor235(L, &a, &b, &c))
 		return -1;
-	if (!best_chain(a, b, c, radices, nstages))
+	if (!best_chain(a, b, c, allowed, radices, nstages))
 		return -1;
 	for (i = 0; i < *nstages; i++)
 		for (j = i + 1; j < *nstages; j++)
@@ -112,6 +119,11 @@ int fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages)
 				radices[j] = t;
 			}
 	return 0;
+}
+
+int fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages)
+{
+	return plan_chain_set(L, FGK_ALL_RADICES, radices, nstages);
 }
 
 /* Register budget: complex elements one thread holds per stage. Must match
@@ -137,22 +149,38 @@ static void fill_chain(fgk_chain *ch, const uint32_t *rad, uint32_t n, uint32_t 
 
 /* Fills everything but the device pointers. Returns 0, or -1 when L has no
  * chain or does not fit in max_smem_bytes of shared memory. */
-int fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes)
+int fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes,
+                      const uint32_t *forced_radices, uint32_t forced_n)
 {
-	uint32_t rad[FGK_MAX_STAGES], rev[FGK_MAX_STAGES], n, s, T = 0, emax = 16, slots, pad;
+	uint32_t rad[FGK_MAX_STAGES], rev[FGK_MAX_STAGES], n, s, T = 0, emax = 16, slots, pad, set;
+	static const uint32_t sets[2] = {FGK_ALL_RADICES, FGK_SMALL_RADICES};
 	memset(p, 0, sizeof(*p));
-	if (fgk_plan_chain(L, rad, &n))
-		return -1;
-	for (;;) {
-		T = 1;
-		for (s = 0; s < n; s++) {
-			uint32_t need = (L / rad[s] + bmax(rad[s], emax) - 1) / bmax(rad[s], emax);
-			if (need > T)
-				T = need;
+	for (set = 0; set < 2; set++) {
+		if (forced_radices) {
+			uint32_t prod = 1;
+			if (forced_n == 0 || forced_n > FGK_MAX_STAGES)
+				return -1;
+			for (n = 0; n < forced_n; n++) {
+				rad[n] = forced_radices[n];
+				prod *= rad[n];
+			}
+			if (prod != L)
+				return -1;
+		} else if (plan_chain_set(L, sets[set], rad, &n)) {
+			return -1;
 		}
-		if (T <= 1024 || emax == 32)
+		for (emax = 16;; emax = 32) {
+			T = 1;
+			for (s = 0; s < n; s++) {
+				uint32_t need = (L / rad[s] + bmax(rad[s], emax) - 1) / bmax(rad[s], emax);
+				if (need > T)
+					T = need;
+			}
+			if (T <= 1024 || emax == 32)
+				break;
+		}
+		if (T <= 1024)
 			break;
-		emax = 32;
 	}
 	if (T > 1024)
 		return -1;

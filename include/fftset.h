@@ -104,10 +104,12 @@ int         fftset_clear_error(struct fftset *fc);           /* returns the code
 int         fftset_cuda_error(const struct fftset *fc);      /* cudaError_t of the last CUDA failure */
 const char *fftset_error_string(int code);
 
-/* CUDA stream (a cudaStream_t) every call of fc is ordered on; NULL = the
- * stream fftset_init created. */
+/* CUDA stream (a cudaStream_t) every call of fc is ordered on. The default
+ * is a non-blocking stream fftset_init creates (fftset_own_stream); NULL is
+ * CUDA's legacy default stream, as everywhere in CUDA. */
 int  fftset_set_stream(struct fftset *fc, void *cuda_stream);
 void *fftset_get_stream(const struct fftset *fc);
+void *fftset_own_stream(const struct fftset *fc);
 /* 1 (default): calls return after their results are in place. 0: calls
  * with device buffers only enqueue work on the stream. */
 int  fftset_set_blocking(struct fftset *fc, int blocking);
@@ -138,6 +140,22 @@ int fftset_fft_conv_batch(const struct fftset_fft *fft, float *output_buf, size_
                           const float *input_buf, size_t in_stride, const float *kernel_buf, unsigned count);
 int fftset_fft_conv_get_kernel_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
                                      const float *input_buf, size_t in_stride, unsigned count);
+
+/* Kernel variants and autotuning. Batched calls of `op` (FFTSET_OP_*) with
+ * enough blocks run one of several compiled kernels for the plan's size
+ * (radix order, threads per transform, transforms per CTA); variant -1 is
+ * the generic kernel. fftset_fft_autotune times every candidate on `count`
+ * blocks of scratch device memory and keeps the fastest (its time in
+ * *best_ms when non-NULL). Not thread-safe with calls on the same plan. */
+#define FFTSET_OP_FORWARD     0
+#define FFTSET_OP_INVERSE     1
+#define FFTSET_OP_GET_KERNEL  2
+#define FFTSET_OP_CONV        3
+#define FFTSET_OP_CORR        4
+int fftset_fft_variants(const struct fftset_fft *fft);
+int fftset_fft_variant(const struct fftset_fft *fft, int op);
+int fftset_fft_set_variant(const struct fftset_fft *fft, int op, int variant);
+int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, float *best_ms);
 
 /* Private Parts
  * ---------------------------------------------------------------------------

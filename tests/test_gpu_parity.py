@@ -270,3 +270,85 @@ def test_other_simd_layouts(fftset_lib, golden_layouts, vw):
             assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
     finally:
         S.close()
+
+
+STATIC = [(1, 1536), (1, 4096), (0, 1024)]
+
+
+@pytest.mark.parametrize("mod,L", STATIC)
+@pytest.mark.parametrize("pad", [0, 2])
+def test_compiled_size_kernels(fftset_lib, gpu_set, mod, L, pad):
+    """Every compile-time kernel variant of the hot sizes (persistent CTAs,
+    tables staged in shared memory), on batches large enough to select them:
+    forward, inverse and convolution against FP64, with padded strides that
+    leave blocks only 8-byte aligned, and in place."""
+    import torch
+    fs = fftset_lib
+    f = gpu_set.create_fft(mod, L)
+    assert f.variants >= 1
+    rng = np.random.default_rng(L + pad)
+    B = 300
+    x = rng.standard_normal((B, 2 * L + pad)).astype(np.float32)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    xd = dev(x)
+    xs = x[:, :2 * L]
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    want_fwd = O.forward64(mod, xs)
+    want_conv = O.conv64(mod, xs, h)
+    ran = 0
+    try:
+        for v in range(-1, f.variants):
+            for op in (fs.OP_FORWARD, fs.OP_INVERSE, fs.OP_CONV):
+                try:
+                    f.set_variant(op, v)
+                except fs.FftsetError:
+                    continue
+                if op == fs.OP_FORWARD:
+                    X = torch.full((B, 2 * L + pad), 5.0, device="cuda")
+                    f.forward_batch(X, xd)
+                    Xh = host(X)
+                    assert np.all(Xh[:, 2 * L:] == 5.0)
+                    assert O.rel_l2(Xh[:, :2 * L], want_fwd) <= tol(mod, L), v
+                elif op == fs.OP_INVERSE:
+                    Xd = dev(np.pad(want_fwd.astype(np.float32), ((0, 0), (0, pad))))
+                    r = torch.empty_like(Xd)
+                    f.inverse_batch(r, Xd)
+                    assert O.rel_l2(host(r)[:, :2 * L], O.inverse64(mod, want_fwd)) <= tol(mod, L), v
+                else:
+                    y = torch.empty_like(xd)
+                    f.conv_batch(y, xd, K)
+                    assert O.rel_l2(host(y)[:, :2 * L], want_conv) <= tol(mod, L), v
+                    buf = xd.clone()
+                    f.conv_batch(buf, buf, K)
+                    assert O.rel_l2(host(buf)[:, :2 * L], want_conv) <= tol(mod, L), v
+                ran += 1
+    finally:
+        for op in (fs.OP_FORWARD, fs.OP_INVERSE, fs.OP_CONV):
+            f.set_variant(op, 0 if f.variants else -1) if _supports(f, op, 0) else None
+    assert ran >= 4
+
+
+def _supports(f, op, v):
+    try:
+        f.set_variant(op, v)
+        return True
+    except Exception:
+        return False
+
+
+def test_autotune_picks_a_working_kernel(fftset_lib, gpu_set):
+    import torch
+    fs = fftset_lib
+    f = gpu_set.create_fft(1, 1536)
+    ms = f.autotune(fs.OP_CONV, 2048)
+    assert ms > 0
+    assert -1 <= f.variant(fs.OP_CONV) < f.variants
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((512, 3072)).astype(np.float32)
+    h = rng.standard_normal(3072).astype(np.float32)
+    K = torch.empty(3072, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    y = torch.empty(512, 3072, device="cuda")
+    f.conv_batch(y, dev(x), K)
+    assert O.rel_l2(host(y), O.conv64(1, x, h)) <= tol(1, 1536)
