@@ -194,8 +194,9 @@ def run_gb300(args):
         f.conv_batch(y, x, K)
 
     # autotune: every compiled kernel for this size, plus the generic one
+    # (--variant V pins one kernel instead)
     sweep = {}
-    for v in range(-1, f.variants):
+    for v in (range(-1, f.variants) if args.variant is None else []):
         try:
             f.set_variant(fs.OP_CONV, v)
         except fs.FftsetError:
@@ -209,7 +210,11 @@ def run_gb300(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         sweep[str(v)] = ev0.elapsed_time(ev1) / 10
-    tuned_ms = f.autotune(fs.OP_CONV, BLOCKS)
+    if args.variant is None:
+        tuned_ms = f.autotune(fs.OP_CONV, BLOCKS)
+    else:
+        f.set_variant(fs.OP_CONV, args.variant)
+        tuned_ms = None
     variant = f.variant(fs.OP_CONV)
 
     for _ in range(max(args.warmup, 3)):
@@ -303,6 +308,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--variant", type=int, default=None,
+                    help="pin the conv kernel variant (-1 generic) instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

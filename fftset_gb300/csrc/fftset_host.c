@@ -68,6 +68,8 @@ struct fs_impl {
 	int                num_sms;
 	struct fftset_fft *first;
 	pthread_mutex_t    lock;
+	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
+	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
 };
@@ -124,6 +126,17 @@ int fftset_init(struct fftset *fc)
 		free(fs);
 		return -1;
 	}
+	if (cudaHostAlloc((void **)&fs->host_flag, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+	    cudaHostGetDevicePointer((void **)&fs->dev_flag, fs->host_flag, 0) != cudaSuccess) {
+		cudaGetLastError();
+		if (fs->host_flag)
+			cudaFreeHost(fs->host_flag);
+		pthread_mutex_destroy(&fs->lock);
+		cudaStreamDestroy(fs->own_stream);
+		free(fs);
+		return -1;
+	}
+	*fs->host_flag = 0;
 	fs->stream = fs->own_stream;
 	fs->blocking = 1;
 	fs->layout_vw = 4;
@@ -150,6 +163,7 @@ void fftset_destroy(struct fftset *fc)
 	for (i = 0; i < FS_NSTAGE; i++)
 		cudaFree(fs->stage[i]);
 	cudaStreamDestroy(fs->own_stream);
+	cudaFreeHost(fs->host_flag);
 	pthread_mutex_destroy(&fs->lock);
 	free(fs);
 	fc->impl = NULL;
@@ -200,8 +214,8 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 		nvar = FS_MAX_VAR;
 	f->nvar = 0;
 	for (v = 0; v < nvar; v++) {
-		uint32_t rad[FGK_MAX_STAGES], n, threads, groups, ops;
-		if (!fgk_static_info(modulation, L, v, rad, &n, &threads, &groups, &ops) ||
+		uint32_t rad[FGK_MAX_STAGES], n, threads, groups, ops, tma;
+		if (!fgk_static_info(modulation, L, v, rad, &n, &threads, &groups, &ops, &tma) ||
 		    fgk_plan_resident(&f->vp[v], L, modulation, fs->max_smem, rad, n))
 			return FFTSET_E_UNSUPPORTED;
 		f->vops[v] = ops;
@@ -372,6 +386,16 @@ static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 	return FFTSET_OK;
 }
 
+/* A kernel whose bounded wait gave up wrote 1 to the mapped flag. */
+static int fs_check_flag(struct fs_impl *fs)
+{
+	if (*(volatile int *)fs->host_flag) {
+		*(volatile int *)fs->host_flag = 0;
+		return fs_latch(fs, FFTSET_E_TIMEOUT, 0);
+	}
+	return FFTSET_OK;
+}
+
 /* Kernel choice: the compile-time kernel when one exists and the batch is
  * large enough to amortise its per-CTA table staging; the generic resident
  * kernel otherwise. */
@@ -383,9 +407,17 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 	struct fs_impl *fs = f->fs;
 	if (v >= 0 && v < f->nvar) {
 		int rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, fs->stream,
-		                           fs->num_sms);
+		                           fs->num_sms, fs->dev_flag);
 		if (rc >= 0)
 			return rc;
+		/* the variant cannot take these buffers (alignment): any other
+		 * compiled variant that can, else the generic kernel */
+		for (v = 0; v < f->nvar; v++) {
+			rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, fs->stream,
+			                       fs->num_sms, fs->dev_flag);
+			if (rc >= 0)
+				return rc;
+		}
 	}
 	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
 }
@@ -429,8 +461,11 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		rc = fs_launch(f, op, out, in, kern, count, in_stride, out_stride);
 		if (rc)
 			return fs_latch(fs, FFTSET_E_CUDA, rc);
-		if (fs->blocking)
-			return fs_cuda(fs, cudaStreamSynchronize(fs->stream));
+		if (fs->blocking) {
+			if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) != 0)
+				return rc;
+			return fs_check_flag(fs);
+		}
 		return FFTSET_OK;
 	}
 
@@ -475,6 +510,8 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		}
 	}
 	rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream));
+	if (rc == FFTSET_OK)
+		rc = fs_check_flag(fs);
 done:
 	if (staged)
 		pthread_mutex_unlock(&fs->lock);
@@ -563,7 +600,10 @@ unsigned fftset_recommend_conv_length(unsigned kernel_length, unsigned max_block
 int fftset_last_error(const struct fftset *fc)
 {
 	struct fs_impl *fs = fs_of(fc);
-	return fs ? fs->err : FFTSET_E_INVALID;
+	if (!fs)
+		return FFTSET_E_INVALID;
+	fs_check_flag(fs); /* picks up kernel reports of non-blocking calls once they finished */
+	return fs->err;
 }
 
 int fftset_clear_error(struct fftset *fc)
@@ -592,6 +632,7 @@ const char *fftset_error_string(int code)
 	case FFTSET_E_NOMEM: return "out of memory";
 	case FFTSET_E_CUDA: return "CUDA error";
 	case FFTSET_E_UNSUPPORTED: return "unsupported operation for this plan";
+	case FFTSET_E_TIMEOUT: return "a bounded wait inside a kernel gave up";
 	default: return "unknown error";
 	}
 }

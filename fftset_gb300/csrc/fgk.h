@@ -80,9 +80,11 @@ uint32_t fgk_max_resident_L(void);
  * variant does not implement op. */
 int fgk_static_count(uint32_t modulation, uint32_t L);
 int fgk_static_info(uint32_t modulation, uint32_t L, int v, uint32_t *radices, uint32_t *n, uint32_t *threads,
-                    uint32_t *groups, uint32_t *opmask);
+                    uint32_t *groups, uint32_t *opmask, uint32_t *tma);
+/* err_flag: device-visible int set to 1 when a bounded wait inside the
+ * kernel gives up (may be NULL) */
 int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
-                      uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms);
+                      uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms, int *err_flag);
 
 #ifdef __cplusplus
 }

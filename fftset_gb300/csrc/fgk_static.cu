@@ -29,7 +29,7 @@ extern "C" int fgk_static_count(uint32_t mod, uint32_t L)
 }
 
 extern "C" int fgk_static_info(uint32_t mod, uint32_t L, int v, uint32_t *radices, uint32_t *n, uint32_t *threads,
-                               uint32_t *groups, uint32_t *opmask)
+                               uint32_t *groups, uint32_t *opmask, uint32_t *tma)
 {
 	const fgk::StaticEntry *e;
 	int nv = fgk::variants(mod, L, &e);
@@ -41,6 +41,7 @@ extern "C" int fgk_static_info(uint32_t mod, uint32_t L, int v, uint32_t *radice
 	*n = e->n;
 	*threads = e->T;
 	*groups = e->G;
+	*tma = e->tma;
 	*opmask = 0;
 	for (int op = 0; op < FGK_OP_COUNT; op++)
 		if (e->fn[op])
@@ -49,7 +50,8 @@ extern "C" int fgk_static_info(uint32_t mod, uint32_t L, int v, uint32_t *radice
 }
 
 extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
-                                 uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms)
+                                 uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms,
+                                 int *err_flag)
 {
 	using namespace fgk;
 	const StaticEntry *e;
@@ -57,6 +59,9 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 	if (v < 0 || v >= nv || op < 0 || op >= FGK_OP_COUNT || !e[v].fn[op])
 		return -1; /* not handled: caller falls back to the generic kernel */
 	e += v;
+	/* bulk copies need 16-byte aligned blocks */
+	if (e->tma && ((((uintptr_t)in) & 15) || ((in_stride * sizeof(float)) & 15)))
+		return -1;
 	if (count == 0)
 		return 0;
 	const size_t smem = e->smem[op];
@@ -73,7 +78,7 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 	uint64_t grid = (uint64_t)per_sm * (uint64_t)num_sms;
 	if (grid > need)
 		grid = need;
-	StaticArgs a{out, in, kern, count, in_stride, out_stride};
+	StaticArgs a{out, in, kern, count, in_stride, out_stride, err_flag};
 	e->fn[op]<<<(unsigned)grid, e->T * e->G, smem, (cudaStream_t)stream>>>(*p, a);
 	return (int)cudaGetLastError();
 }

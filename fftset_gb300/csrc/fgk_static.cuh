@@ -26,9 +26,10 @@
 
 namespace fgk {
 
-template <int MOD_, int L_, int T_, int G_, int TWG_, int... Rs> struct SCfg {
+template <int MOD_, int L_, int T_, int G_, int TWG_, int TMA_, int... Rs> struct SCfg {
 	static constexpr int MOD = MOD_;
 	static constexpr bool TWG = TWG_ != 0; /* twiddles read from global memory (L1) instead of shared */
+	static constexpr bool TMA = TMA_ != 0; /* inputs double-buffered by bulk copies */
 	static constexpr int L = L_;
 	static constexpr int T = T_;
 	static constexpr int G = G_;
@@ -191,168 +192,316 @@ struct StaticArgs {
 	const float *kern;
 	uint32_t     count;
 	size_t       in_stride, out_stride;
+	int         *err; /* set to 1 when a bounded wait gives up (TMA mode) */
 };
 
+/* ---- TMA (cp.async.bulk) + mbarrier helpers ---------------------------- */
+#define FGK_SPIN_LIMIT (1u << 20) /* x 1 us suspend hint: about a second */
+
+__device__ __forceinline__ uint32_t smem_u32(const void *ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+/* one 1-D bulk copy global -> shared, completion counted on `bar` */
+__device__ __forceinline__ void tma_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smem_u32(dst)),
+	             "l"(src), "r"(bytes), "r"(smem_u32(bar))
+	             : "memory");
+}
+
+/* bounded wait for phase `parity` of `bar`; false when it gave up */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+	for (uint32_t it = 0; it < FGK_SPIN_LIMIT; it++) {
+		uint32_t ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+		             "selp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok)
+		             : "r"(smem_u32(bar)), "r"(parity), "r"(1000u)
+		             : "memory");
+		if (ok)
+			return true;
+	}
+	return false;
+}
+
+/* ---- one transform ----------------------------------------------------- */
+/* First-stage loader: the modulated sequence (FORWARD/CONV) or conj(W)
+ * (INVERSE) at natural index i, from HBM (x is a global pointer) or from the
+ * block's shared staging copy (x is a shared pointer). */
+template <class C, int OP, bool SHARED_IN> struct FirstLoad {
+	const float  *x;
+	const float2 *mods;
+	__device__ __forceinline__ float ld(int i) const
+	{
+		if constexpr (SHARED_IN)
+			return x[i];
+		else
+			return ldcs(x + i);
+	}
+	__device__ __forceinline__ float2 ld2(int i) const
+	{
+		const float2 *x2 = reinterpret_cast<const float2 *>(x);
+		if constexpr (SHARED_IN)
+			return x2[i];
+		else
+			return ldcs2(x2 + i);
+	}
+	__device__ __forceinline__ float2 operator()(int i) const
+	{
+		constexpr int L = C::L;
+		if constexpr (OP == FGK_OP_INVERSE) {
+			if constexpr (C::MOD == FGK_MOD_FREQOFF)
+				return i < ((L + 1) >> 1) ? conjf2(ld2(2 * i)) : ld2(2 * (L - 1 - i) + 1);
+			else
+				return conjf2(ld2(i));
+		} else {
+			if constexpr (C::MOD == FGK_MOD_FREQOFF)
+				return cmul(make_float2(ld(i), -ld(L + i)), mods[i]);
+			else
+				return ld2(i);
+		}
+	}
+};
+
+/* Runs one transform. `first` feeds stage 0; when stage 0 reads the same
+ * shared buffer it writes (TMA mode), IN_PLACE adds the barrier between its
+ * loads and stores. Ends with the group barrier that frees `ex`. */
+template <class C, int OP, bool IN_PLACE, class First>
+__device__ __forceinline__ void transform(int tid, int g, const Ex<C> &ex, const First &first, float *y,
+                                          const float2 *tws, const float2 *mods, const float2 *ks)
+{
+	constexpr int L = C::L, N = C::N;
+	constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
+	constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
+	auto out_final = [&](int i, float2 u) {
+		if constexpr (FREQ) {
+			const float2 r = cmul(u, mods[i]);
+			stcs(y + i, r.x);
+			stcs(y + L + i, r.y);
+		} else {
+			stcs2(reinterpret_cast<float2 *>(y) + i, conjf2(u));
+		}
+	};
+	auto exput = [&](int i, float2 v) { ex.put(i, v); };
+	{
+		constexpr int R = C::fr(0);
+		Tile<C, R> t0;
+		t0.load(tid, first);
+		if constexpr (IN_PLACE)
+			gsync<C>(g);
+		t0.template butterfly<1>(tid, tws);
+		t0.template store<1>(tid, exput);
+		gsync<C>(g);
+	}
+	fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
+	if constexpr (CONV) {
+		static_assert(N >= 2, "static conv needs two or more stages");
+		{
+			/* last forward stage + product + first reversed stage */
+			constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
+			Tile<C, R> t;
+			t.load(tid, ex);
+			gsync<C>(g);
+			t.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
+#pragma unroll
+			for (int b = 0; b < Tile<C, R>::NB; b++) {
+				const int j = tid + b * C::T;
+				if (Tile<C, R>::live(tid, b)) {
+#pragma unroll
+					for (int q = 0; q < R; q++)
+						t.v[b][q] = conjf2(cmul(t.v[b][q], ks[j + q * (L / R)]));
+					Radix<R>::run(t.v[b]);
+				}
+			}
+			t.template store<1>(tid, exput);
+			gsync<C>(g);
+		}
+		inv_mid<C, 1, N - 1>(tid, g, ex, tws);
+		{
+			constexpr int R = C::ir(N - 1), NS = C::ins(N - 1);
+			Tile<C, R> t;
+			t.load(tid, ex);
+			t.template butterfly<NS>(tid, tws + C::itw_off(N - 1));
+			t.template store<NS>(tid, out_final);
+		}
+	} else {
+		constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
+		Tile<C, R> t;
+		t.load(tid, ex);
+		if constexpr (OP == FGK_OP_FORWARD && FREQ)
+			gsync<C>(g); /* results go back to shared memory */
+		t.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
+		if constexpr (OP == FGK_OP_INVERSE) {
+			t.template store<NS>(tid, out_final);
+		} else if constexpr (!FREQ) {
+			t.template store<NS>(tid, [&](int i, float2 v) { stcs2(reinterpret_cast<float2 *>(y) + i, v); });
+		} else {
+			t.template store<NS>(tid, exput);
+			gsync<C>(g);
+			/* X[2m] = W[m], X[2m+1] = conj W[L-1-m] */
+			if ((reinterpret_cast<uintptr_t>(y) & 15) == 0) {
+				float4 *y4 = reinterpret_cast<float4 *>(y);
+				for (int m = tid; m < L / 2; m += C::T) {
+					const float2 w0 = ex(m), w1 = ex(L - 1 - m);
+					__stcs(y4 + m, make_float4(w0.x, w0.y, w1.x, -w1.y));
+				}
+			} else {
+				float2 *y2 = reinterpret_cast<float2 *>(y);
+				for (int m = tid; m < L / 2; m += C::T) {
+					const float2 w0 = ex(m), w1 = ex(L - 1 - m);
+					stcs2(y2 + 2 * m, w0);
+					stcs2(y2 + 2 * m + 1, conjf2(w1));
+				}
+			}
+		}
+	}
+	gsync<C>(g); /* the exchange buffer is reused by the next transform */
+}
+
+/* ---- per-CTA tables ----------------------------------------------------- */
+template <class C, int OP>
+__device__ __forceinline__ void stage_tables(const fgk_plan &p, const StaticArgs &a, float2 *smem, float2 *mods,
+                                             float2 *ks)
+{
+	constexpr int L = C::L;
+	if constexpr (!C::TWG)
+		stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
+	if constexpr (C::MOD == FGK_MOD_FREQOFF) {
+		const float2 *gm = (const float2 *)p.modtw;
+		for (int i = threadIdx.x; i < L; i += blockDim.x)
+			mods[i] = __ldg(gm + i);
+	}
+	if constexpr (OP == FGK_OP_CONV || OP == FGK_OP_CORR) {
+		const int32_t *kidx = p.kidx;
+		const int kvw = (int)p.kvw;
+		for (int i = threadIdx.x; i < L; i += blockDim.x) {
+			const int o = __ldg(kidx + i);
+			float2 k = make_float2(__ldg(a.kern + o), __ldg(a.kern + o + kvw));
+			if (OP == FGK_OP_CORR)
+				k.y = -k.y;
+			ks[i] = k;
+		}
+	}
+}
+
+template <class C, int OP> struct Layout {
+	static constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
+	static constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
+	static constexpr size_t TW = C::TWG ? 0 : (size_t)C::TW_TOTAL; /* float2 */
+	static constexpr size_t MODS = FREQ ? C::L : 0;
+	static constexpr size_t KS = CONV ? C::L : 0;
+	static constexpr size_t TABLES = TW + MODS + KS;
+	/* TMA mode: per group two buffers, each holding a raw input block (2L
+	 * floats) or the padded exchange buffer, whichever is larger; 16-byte
+	 * multiples so every bulk copy lands aligned */
+	static constexpr size_t BUF = ((C::SLOTS > C::L ? C::SLOTS : C::L) + 1) & ~(size_t)1; /* float2 */
+	static constexpr size_t DIRECT_BYTES = sizeof(float2) * (TABLES + (size_t)C::G * C::SLOTS);
+	static constexpr size_t TMA_BYTES = sizeof(float2) * (((TABLES + 1) & ~(size_t)1) + 2 * (size_t)C::G * BUF) +
+	                                    2 * (size_t)C::G * sizeof(uint64_t);
+};
+
+/* ---- kernels ------------------------------------------------------------ */
 template <class C, int OP>
 __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel(const fgk_plan p, StaticArgs a)
 {
 	extern __shared__ float2 smem[];
-	constexpr int L = C::L, N = C::N;
-	constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
-	constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
-	/* twiddles: staged in shared memory ([p-1][k] per stage), or read from
-	 * the plan's global table ([k][p-1] per stage) through L1 */
+	using Lay = Layout<C, OP>;
 	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
-	float2 *mods = smem + (C::TWG ? 0 : C::TW_TOTAL);     /* L (FREQ) */
-	float2 *ks = mods + (FREQ ? L : 0);                   /* L (CONV) */
-	float2 *exb = ks + (CONV ? L : 0);                    /* G * SLOTS */
-
-	/* ---- stage the tables once per CTA ---- */
-	{
-		if constexpr (!C::TWG)
-			stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
-		if constexpr (FREQ) {
-			const float2 *gm = (const float2 *)p.modtw;
-			for (int i = threadIdx.x; i < L; i += blockDim.x)
-				mods[i] = __ldg(gm + i);
-		}
-		if constexpr (CONV) {
-			const int32_t *kidx = p.kidx;
-			const int kvw = (int)p.kvw;
-			for (int i = threadIdx.x; i < L; i += blockDim.x) {
-				const int o = __ldg(kidx + i);
-				float2 k = make_float2(__ldg(a.kern + o), __ldg(a.kern + o + kvw));
-				if (OP == FGK_OP_CORR)
-					k.y = -k.y;
-				ks[i] = k;
-			}
-		}
-		__syncthreads();
-	}
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *exb = ks + Lay::KS;
+	stage_tables<C, OP>(p, a, smem, mods, ks);
+	__syncthreads();
 
 	const int g = threadIdx.x / C::T;
 	const int tid = threadIdx.x - g * C::T;
 	const Ex<C> ex{exb + (size_t)g * C::SLOTS};
-
 	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {
-		const float *x = a.in + t * a.in_stride;
-		float *y = a.out + t * a.out_stride;
-
-		/* first stage input */
-		auto in_fwd = [&](int i) -> float2 {
-			if constexpr (FREQ)
-				return cmul(make_float2(ldcs(x + i), -ldcs(x + L + i)), mods[i]);
-			else
-				return ldcs2(reinterpret_cast<const float2 *>(x) + i);
-		};
-		auto in_inv = [&](int i) -> float2 {
-			const float2 *X = reinterpret_cast<const float2 *>(x);
-			if constexpr (FREQ)
-				return i < ((L + 1) >> 1) ? conjf2(ldcs2(X + 2 * i)) : ldcs2(X + 2 * (L - 1 - i) + 1);
-			else
-				return conjf2(ldcs2(X + i));
-		};
-		/* final output from u = DFT(conj(.)) */
-		auto out_final = [&](int i, float2 u) {
-			if constexpr (FREQ) {
-				const float2 r = cmul(u, mods[i]);
-				stcs(y + i, r.x);
-				stcs(y + L + i, r.y);
-			} else {
-				stcs2(reinterpret_cast<float2 *>(y) + i, conjf2(u));
-			}
-		};
-		auto exput = [&](int i, float2 v) { ex.put(i, v); };
-
-		if constexpr (CONV) {
-			static_assert(N >= 2, "static conv needs two or more stages");
-			{
-				constexpr int R = C::fr(0);
-				Tile<C, R> t0;
-				t0.load(tid, in_fwd);
-				t0.template butterfly<1>(tid, tws);
-				t0.template store<1>(tid, exput);
-				gsync<C>(g);
-			}
-			fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
-			{
-				/* last forward stage + product + first reversed stage */
-				constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
-				Tile<C, R> t;
-				t.load(tid, ex);
-				gsync<C>(g);
-				t.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
-#pragma unroll
-				for (int b = 0; b < Tile<C, R>::NB; b++) {
-					const int j = tid + b * C::T;
-					if (Tile<C, R>::live(tid, b)) {
-#pragma unroll
-						for (int q = 0; q < R; q++)
-							t.v[b][q] = conjf2(cmul(t.v[b][q], ks[j + q * (L / R)]));
-						Radix<R>::run(t.v[b]);
-					}
-				}
-				t.template store<1>(tid, exput);
-				gsync<C>(g);
-			}
-			inv_mid<C, 1, N - 1>(tid, g, ex, tws);
-			{
-				constexpr int R = C::ir(N - 1), NS = C::ins(N - 1);
-				Tile<C, R> t;
-				t.load(tid, ex);
-				t.template butterfly<NS>(tid, tws + C::itw_off(N - 1));
-				t.template store<NS>(tid, out_final);
-			}
-		} else {
-			/* forward chain on the modulated input (FORWARD) or on conj(W) (INVERSE) */
-			{
-				constexpr int R = C::fr(0);
-				Tile<C, R> t0;
-				if constexpr (OP == FGK_OP_INVERSE)
-					t0.load(tid, in_inv);
-				else
-					t0.load(tid, in_fwd);
-				t0.template butterfly<1>(tid, tws);
-				t0.template store<1>(tid, exput);
-				gsync<C>(g);
-			}
-			fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
-			{
-				constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
-				Tile<C, R> t;
-				t.load(tid, ex);
-				if constexpr (OP == FGK_OP_FORWARD && FREQ)
-					gsync<C>(g); /* results go back to shared memory */
-				t.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
-				if constexpr (OP == FGK_OP_INVERSE) {
-					t.template store<NS>(tid, out_final);
-				} else if constexpr (!FREQ) {
-					t.template store<NS>(tid, [&](int i, float2 v) {
-						stcs2(reinterpret_cast<float2 *>(y) + i, v);
-					});
-				} else {
-					t.template store<NS>(tid, exput);
-					gsync<C>(g);
-					/* X[2m] = W[m], X[2m+1] = conj W[L-1-m] */
-					if ((reinterpret_cast<uintptr_t>(y) & 15) == 0) {
-						float4 *y4 = reinterpret_cast<float4 *>(y);
-						for (int m = tid; m < L / 2; m += C::T) {
-							const float2 w0 = ex(m), w1 = ex(L - 1 - m);
-							__stcs(y4 + m, make_float4(w0.x, w0.y, w1.x, -w1.y));
-						}
-					} else {
-						float2 *y2 = reinterpret_cast<float2 *>(y);
-						for (int m = tid; m < L / 2; m += C::T) {
-							const float2 w0 = ex(m), w1 = ex(L - 1 - m);
-							stcs2(y2 + 2 * m, w0);
-							stcs2(y2 + 2 * m + 1, conjf2(w1));
-						}
-					}
-				}
-			}
-		}
-		gsync<C>(g); /* the exchange buffer is reused by the next transform */
+		const FirstLoad<C, OP, false> first{a.in + t * a.in_stride, mods};
+		transform<C, OP, false>(tid, g, ex, first, a.out + t * a.out_stride, tws, mods, ks);
 	}
+}
+
+/* TMA mode: each group double-buffers its input blocks with bulk copies
+ * (one elected thread issues them), so the next block streams in while the
+ * current one is transformed; the block's staging buffer then serves as its
+ * exchange buffer. Requires 16-byte aligned blocks. */
+template <class C, int OP>
+__global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_tma(const fgk_plan p, StaticArgs a)
+{
+	extern __shared__ float2 smem[];
+	using Lay = Layout<C, OP>;
+	constexpr uint32_t BYTES = 2u * C::L * sizeof(float);
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *bufs = smem + ((Lay::TABLES + 1) & ~(size_t)1);
+	uint64_t *bars = reinterpret_cast<uint64_t *>(bufs + 2 * (size_t)C::G * Lay::BUF);
+	__shared__ int grp_err[C::G];
+
+	const int g = threadIdx.x / C::T;
+	const int tid = threadIdx.x - g * C::T;
+	if (threadIdx.x < 2 * C::G)
+		mbar_init(bars + threadIdx.x, 1);
+	if (threadIdx.x < C::G)
+		grp_err[threadIdx.x] = 0;
+	mbar_fence_init();
+	stage_tables<C, OP>(p, a, smem, mods, ks);
+	__syncthreads();
+
+	const uint64_t step = (uint64_t)gridDim.x * C::G;
+	uint64_t t = (uint64_t)blockIdx.x * C::G + g;
+	/* group g owns buffers 2g, 2g+1 and barriers 2g, 2g+1 (computed, not
+	 * held in arrays: a runtime-indexed array would live in local memory) */
+	float2 *const gbuf = bufs + (size_t)(2 * g) * Lay::BUF;
+	uint64_t *const gbar = bars + 2 * g;
+	uint32_t pending = 0; /* bit b: copy into buffer b issued, not yet waited for */
+	if (t < a.count) {
+		if (tid == 0)
+			tma_load(gbuf, a.in + t * a.in_stride, BYTES, gbar);
+		pending = 1;
+	}
+	uint32_t it = 0;
+	for (; t < a.count; t += step, it++) {
+		const uint32_t b = it & 1;
+		const bool ok = mbar_wait(gbar + b, (it >> 1) & 1);
+		if (!ok) {
+			grp_err[g] = 1;
+			if (a.err)
+				atomicExch(a.err, 1);
+		}
+		pending = ok ? (pending & ~(1u << b)) : pending; /* a copy that never signalled is drained below */
+		if (t + step < a.count) {
+			/* the other buffer served the previous block, released by its final barrier */
+			if (tid == 0) {
+				fence_proxy_async();
+				tma_load(gbuf + (size_t)(b ^ 1) * Lay::BUF, a.in + (t + step) * a.in_stride, BYTES, gbar + (b ^ 1));
+			}
+			pending |= 1u << (b ^ 1);
+		}
+		gsync<C>(g);
+		if (grp_err[g])
+			break;
+		float2 *cur = gbuf + (size_t)b * Lay::BUF;
+		const Ex<C> ex{cur};
+		const FirstLoad<C, OP, true> first{reinterpret_cast<const float *>(cur), mods};
+		transform<C, OP, true>(tid, g, ex, first, a.out + t * a.out_stride, tws, mods, ks);
+	}
+	/* drain copies still in flight (only after a failed wait) */
+	for (uint32_t b = 0; b < 2; b++)
+		if (pending & (1u << b))
+			mbar_wait(gbar + b, ((it + (b != (it & 1))) >> 1) & 1);
 }
 
 /* ------------------------------------------------------------------------
@@ -360,7 +509,7 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel(const fgk_plan p,
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
 
 struct StaticEntry {
-	uint32_t  mod, L, T, G, n;
+	uint32_t  mod, L, T, G, n, tma;
 	uint32_t  radices[FGK_MAX_STAGES];
 	size_t    smem[FGK_OP_COUNT];
 	static_fn fn[FGK_OP_COUNT];
@@ -368,10 +517,15 @@ struct StaticEntry {
 
 template <class C, int OP> constexpr size_t smem_bytes()
 {
-	constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
-	constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
-	return sizeof(float2) * ((C::TWG ? 0 : (size_t)C::TW_TOTAL) + (FREQ ? C::L : 0) + (CONV ? C::L : 0) +
-	                         (size_t)C::G * C::SLOTS);
+	return C::TMA ? Layout<C, OP>::TMA_BYTES : Layout<C, OP>::DIRECT_BYTES;
+}
+
+template <class C, int OP> constexpr static_fn kernel_of()
+{
+	if constexpr (C::TMA)
+		return static_kernel_tma<C, OP>;
+	else
+		return static_kernel<C, OP>;
 }
 
 /* OPS: bit mask of the ops compiled for this configuration */
@@ -383,22 +537,23 @@ template <class C, int OPS> StaticEntry make_entry()
 	e.T = C::T;
 	e.G = C::G;
 	e.n = C::N;
+	e.tma = C::TMA ? 1u : 0u;
 	for (int i = 0; i < C::N; i++)
 		e.radices[i] = C::R[i];
 	if constexpr ((OPS >> FGK_OP_FORWARD) & 1) {
-		e.fn[FGK_OP_FORWARD] = static_kernel<C, FGK_OP_FORWARD>;
+		e.fn[FGK_OP_FORWARD] = kernel_of<C, FGK_OP_FORWARD>();
 		e.smem[FGK_OP_FORWARD] = smem_bytes<C, FGK_OP_FORWARD>();
 	}
 	if constexpr ((OPS >> FGK_OP_INVERSE) & 1) {
-		e.fn[FGK_OP_INVERSE] = static_kernel<C, FGK_OP_INVERSE>;
+		e.fn[FGK_OP_INVERSE] = kernel_of<C, FGK_OP_INVERSE>();
 		e.smem[FGK_OP_INVERSE] = smem_bytes<C, FGK_OP_INVERSE>();
 	}
 	if constexpr ((OPS >> FGK_OP_CONV) & 1) {
-		e.fn[FGK_OP_CONV] = static_kernel<C, FGK_OP_CONV>;
+		e.fn[FGK_OP_CONV] = kernel_of<C, FGK_OP_CONV>();
 		e.smem[FGK_OP_CONV] = smem_bytes<C, FGK_OP_CONV>();
 	}
 	if constexpr ((OPS >> FGK_OP_CORR) & 1) {
-		e.fn[FGK_OP_CORR] = static_kernel<C, FGK_OP_CORR>;
+		e.fn[FGK_OP_CORR] = kernel_of<C, FGK_OP_CORR>();
 		e.smem[FGK_OP_CORR] = smem_bytes<C, FGK_OP_CORR>();
 	}
 	return e;

@@ -99,6 +99,7 @@ unsigned fftset_recommend_conv_length(unsigned kernel_length, unsigned max_block
 #define FFTSET_E_NOMEM          2  /* host or device allocation failed */
 #define FFTSET_E_CUDA           3  /* a CUDA call failed; see fftset_cuda_error */
 #define FFTSET_E_UNSUPPORTED    4  /* plan cannot run this operation */
+#define FFTSET_E_TIMEOUT        5  /* a bounded wait inside a kernel gave up (results invalid) */
 int         fftset_last_error(const struct fftset *fc);      /* returns and keeps the latched code */
 int         fftset_clear_error(struct fftset *fc);           /* returns the code and resets it */
 int         fftset_cuda_error(const struct fftset *fc);      /* cudaError_t of the last CUDA failure */
