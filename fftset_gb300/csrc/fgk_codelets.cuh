@@ -23,8 +23,33 @@ static inline float2 make_float2(float a, float b) { float2 r; r.x = a; r.y = b;
 
 namespace fgk {
 
+/* Complex add/sub: on sm_100+ one packed f32x2 instruction (same FP32
+ * throughput as two scalar adds, half the issue slots). */
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+FGK_HD float2 cadd(float2 a, float2 b)
+{
+	unsigned long long ra, rb, rd;
+	float2 r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+	asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(rd));
+	return r;
+}
+FGK_HD float2 csub(float2 a, float2 b)
+{
+	unsigned long long ra, rb, rd;
+	float2 r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+	asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(rd));
+	return r;
+}
+#else
 FGK_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 FGK_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#endif
 FGK_HD float2 cmul(float2 a, float2 w) { return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x); }
 /* a * conj(w) */
 FGK_HD float2 cmulc(float2 a, float2 w) { return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y); }

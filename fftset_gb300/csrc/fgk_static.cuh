@@ -26,10 +26,15 @@
 
 namespace fgk {
 
-template <int MOD_, int L_, int T_, int G_, int TWG_, int TMA_, int... Rs> struct SCfg {
+/* MODE: 0 in-place exchange buffer, direct HBM loads; 1 in-place with
+ * inputs double-buffered by bulk copies (TMA); 2 ping-pong exchange buffers
+ * (out-of-place stages, one barrier per stage, one butterfly at a time) */
+template <int MOD_, int L_, int T_, int G_, int TWG_, int MODE_, int... Rs> struct SCfg {
 	static constexpr int MOD = MOD_;
 	static constexpr bool TWG = TWG_ != 0; /* twiddles read from global memory (L1) instead of shared */
-	static constexpr bool TMA = TMA_ != 0; /* inputs double-buffered by bulk copies */
+	static constexpr int MODE = MODE_;
+	static constexpr bool TMA = MODE_ == 1;
+	static constexpr bool PP = MODE_ == 2;
 	static constexpr int L = L_;
 	static constexpr int T = T_;
 	static constexpr int G = G_;
@@ -407,6 +412,7 @@ template <class C, int OP> struct Layout {
 	 * multiples so every bulk copy lands aligned */
 	static constexpr size_t BUF = ((C::SLOTS > C::L ? C::SLOTS : C::L) + 1) & ~(size_t)1; /* float2 */
 	static constexpr size_t DIRECT_BYTES = sizeof(float2) * (TABLES + (size_t)C::G * C::SLOTS);
+	static constexpr size_t PP_BYTES = sizeof(float2) * (TABLES + 2 * (size_t)C::G * C::SLOTS);
 	static constexpr size_t TMA_BYTES = sizeof(float2) * (((TABLES + 1) & ~(size_t)1) + 2 * (size_t)C::G * BUF) +
 	                                    2 * (size_t)C::G * sizeof(uint64_t);
 };
@@ -504,6 +510,176 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_tma(const fgk_pla
 			mbar_wait(gbar + b, ((it + (b != (it & 1))) >> 1) & 1);
 }
 
+/* ---- ping-pong mode ------------------------------------------------------
+ * One stage = read buffer `src`, write buffer `dst`; butterflies are processed
+ * one at a time (register tile = one radix), and the only barrier is the one
+ * after the stage's stores. */
+template <class C, int R, int NS, class Ld, class St>
+__device__ __forceinline__ void pp_stage(int tid, const float2 *tws, Ld &&ld, St &&st)
+{
+	constexpr int NBF = C::L / R;
+	constexpr int NB = (NBF + C::T - 1) / C::T;
+	constexpr bool FULL = (NBF % C::T) == 0;
+#pragma unroll 2
+	for (int b = 0; b < NB; b++) {
+		const int j = tid + b * C::T;
+		if (FULL || j < NBF) {
+			float2 v[R];
+#pragma unroll
+			for (int p = 0; p < R; p++)
+				v[p] = ld(j + p * NBF);
+			const int k = j % NS;
+			if constexpr (NS > 1) {
+#pragma unroll
+				for (int p = 1; p < R; p++)
+					v[p] = cmul(v[p], C::TWG ? __ldg(tws + k * (R - 1) + (p - 1)) : tws[(p - 1) * NS + k]);
+			}
+			Radix<R>::run(v);
+			const int base = (j - k) * R + k;
+#pragma unroll
+			for (int q = 0; q < R; q++)
+				st(base + q * NS, v[q]);
+		}
+	}
+}
+
+/* forward stages S..E-1 between the two buffers; returns via the template
+ * the buffer parity after the last one (buffers alternate every stage) */
+template <class C, int S, int E>
+__device__ __forceinline__ void pp_fwd(int tid, int g, float2 *buf0, float2 *buf1, const float2 *tws)
+{
+	if constexpr (S < E) {
+		constexpr int R = C::fr(S), NS = C::fns(S);
+		/* stage S reads buffer (S-1)&1 ... stage 0 wrote buffer 0 */
+		const Ex<C> src{((S - 1) & 1) ? buf1 : buf0}, dst{((S - 1) & 1) ? buf0 : buf1};
+		pp_stage<C, R, NS>(tid, tws + C::ftw_off(S), src, [&](int i, float2 v) { dst.put(i, v); });
+		gsync<C>(g);
+		pp_fwd<C, S + 1, E>(tid, g, buf0, buf1, tws);
+	}
+}
+
+/* reversed-chain stages S..E-1; the fused stage (global index N-1) wrote
+ * buffer (N-1)&1, so reversed stage s (global index N-1+s) reads (N-2+s)&1 */
+template <class C, int S, int E>
+__device__ __forceinline__ void pp_inv(int tid, int g, float2 *buf0, float2 *buf1, const float2 *tws)
+{
+	if constexpr (S < E) {
+		constexpr int R = C::ir(S), NS = C::ins(S);
+		constexpr int RD = (C::N - 2 + S) & 1;
+		const Ex<C> src{RD ? buf1 : buf0}, dst{RD ? buf0 : buf1};
+		pp_stage<C, R, NS>(tid, tws + C::itw_off(S), src, [&](int i, float2 v) { dst.put(i, v); });
+		gsync<C>(g);
+		pp_inv<C, S + 1, E>(tid, g, buf0, buf1, tws);
+	}
+}
+
+template <class C, int OP>
+__device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float2 *buf1,
+                                             const FirstLoad<C, OP, false> &first, float *y, const float2 *tws,
+                                             const float2 *mods, const float2 *ks)
+{
+	constexpr int L = C::L, N = C::N;
+	constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
+	constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
+	static_assert(N >= 2, "ping-pong kernels need two or more stages");
+	auto out_final = [&](int i, float2 u) {
+		if constexpr (FREQ) {
+			const float2 r = cmul(u, mods[i]);
+			stcs(y + i, r.x);
+			stcs(y + L + i, r.y);
+		} else {
+			stcs2(reinterpret_cast<float2 *>(y) + i, conjf2(u));
+		}
+	};
+	const Ex<C> b0{buf0};
+	/* stage 0: HBM -> buffer 0 */
+	pp_stage<C, C::fr(0), 1>(tid, tws, first, [&](int i, float2 v) { b0.put(i, v); });
+	gsync<C>(g);
+	pp_fwd<C, 1, N - 1>(tid, g, buf0, buf1, tws);
+	/* stage N-1 reads buffer (N-2)&1 */
+	const Ex<C> src{((N - 2) & 1) ? buf1 : buf0}, dst{((N - 2) & 1) ? buf0 : buf1};
+	if constexpr (CONV) {
+		constexpr int R = C::fr(N - 1), NS = C::fns(N - 1), NBF = L / R;
+		constexpr int NB = (NBF + C::T - 1) / C::T;
+		constexpr bool FULL = (NBF % C::T) == 0;
+#pragma unroll 2
+		for (int b = 0; b < NB; b++) {
+			const int j = tid + b * C::T;
+			if (FULL || j < NBF) {
+				float2 v[R];
+#pragma unroll
+				for (int p = 0; p < R; p++)
+					v[p] = src(j + p * NBF);
+				if constexpr (NS > 1) {
+					const float2 *t = tws + C::ftw_off(N - 1);
+#pragma unroll
+					for (int p = 1; p < R; p++)
+						v[p] = cmul(v[p], C::TWG ? __ldg(t + j * (R - 1) + (p - 1)) : t[(p - 1) * NS + j]);
+				}
+				Radix<R>::run(v);
+#pragma unroll
+				for (int q = 0; q < R; q++)
+					v[q] = conjf2(cmul(v[q], ks[j + q * NBF]));
+				Radix<R>::run(v);
+#pragma unroll
+				for (int q = 0; q < R; q++)
+					dst.put(j * R + q, v[q]);
+			}
+		}
+		gsync<C>(g);
+		pp_inv<C, 1, N - 1>(tid, g, buf0, buf1, tws);
+		constexpr int RL = C::ir(N - 1), NSL = C::ins(N - 1);
+		constexpr int RD = (2 * N - 3) & 1; /* reversed stage N-1 is global stage 2N-2 */
+		const Ex<C> last{RD ? buf1 : buf0};
+		pp_stage<C, RL, NSL>(tid, tws + C::itw_off(N - 1), last, out_final);
+		/* the next transform's stage 0 writes buffer 0: if this stage read
+		 * it, every thread must be done first */
+		if constexpr (RD == 0)
+			gsync<C>(g);
+	} else {
+		constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
+		if constexpr (OP == FGK_OP_INVERSE) {
+			pp_stage<C, R, NS>(tid, tws + C::ftw_off(N - 1), src, out_final);
+		} else if constexpr (!FREQ) {
+			pp_stage<C, R, NS>(tid, tws + C::ftw_off(N - 1), src,
+			                   [&](int i, float2 v) { stcs2(reinterpret_cast<float2 *>(y) + i, v); });
+		} else {
+			pp_stage<C, R, NS>(tid, tws + C::ftw_off(N - 1), src, [&](int i, float2 v) { dst.put(i, v); });
+			gsync<C>(g);
+			/* X[2m] = W[m], X[2m+1] = conj W[L-1-m] */
+			float2 *y2 = reinterpret_cast<float2 *>(y);
+			for (int m = tid; m < L / 2; m += C::T) {
+				const float2 w0 = dst(m), w1 = dst(L - 1 - m);
+				stcs2(y2 + 2 * m, w0);
+				stcs2(y2 + 2 * m + 1, conjf2(w1));
+			}
+		}
+		gsync<C>(g);
+	}
+}
+
+template <class C, int OP>
+__global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_pp(const fgk_plan p, StaticArgs a)
+{
+	extern __shared__ float2 smem[];
+	using Lay = Layout<C, OP>;
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *exb = ks + Lay::KS;
+	stage_tables<C, OP>(p, a, smem, mods, ks);
+	__syncthreads();
+
+	const int g = threadIdx.x / C::T;
+	const int tid = threadIdx.x - g * C::T;
+	float2 *buf0 = exb + (size_t)(2 * g) * C::SLOTS;
+	float2 *buf1 = buf0 + C::SLOTS;
+	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {
+		const FirstLoad<C, OP, false> first{a.in + t * a.in_stride, mods};
+		pp_transform<C, OP>(tid, g, buf0, buf1, first, a.out + t * a.out_stride, tws, mods, ks);
+	}
+}
+
 /* ------------------------------------------------------------------------
  * Registry entries */
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
@@ -517,20 +693,28 @@ struct StaticEntry {
 
 template <class C, int OP> constexpr size_t smem_bytes()
 {
-	return C::TMA ? Layout<C, OP>::TMA_BYTES : Layout<C, OP>::DIRECT_BYTES;
+	return C::TMA ? Layout<C, OP>::TMA_BYTES : C::PP ? Layout<C, OP>::PP_BYTES : Layout<C, OP>::DIRECT_BYTES;
 }
 
 template <class C, int OP> constexpr static_fn kernel_of()
 {
 	if constexpr (C::TMA)
 		return static_kernel_tma<C, OP>;
+	else if constexpr (C::PP)
+		return static_kernel_pp<C, OP>;
 	else
 		return static_kernel<C, OP>;
 }
 
 /* OPS: bit mask of the ops compiled for this configuration */
+/* dynamic shared memory of one CTA must fit the 227 KB opt-in limit, with
+ * room for the few bytes of static shared memory the TMA mode declares */
+constexpr size_t FGK_SMEM_LIMIT = 232448 - 1024;
+
 template <class C, int OPS> StaticEntry make_entry()
 {
+	static_assert(smem_bytes<C, FGK_OP_CONV>() <= FGK_SMEM_LIMIT, "variant exceeds shared memory");
+	static_assert(smem_bytes<C, FGK_OP_FORWARD>() <= FGK_SMEM_LIMIT, "variant exceeds shared memory");
 	StaticEntry e{};
 	e.mod = C::MOD;
 	e.L = C::L;

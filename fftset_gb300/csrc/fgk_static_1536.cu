@@ -6,14 +6,15 @@
 #include "fgk_static.cuh"
 
 namespace fgk {
-/* (16,16,6): R16 stages use 96 of 128 threads, R6 stages two butterflies per
- * thread; (8,8,8,3): 64 threads, 24 values per thread; (16,12,8): one warp
- * per transform, 48 values per thread. */
-using V0 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 4, 0, 1, 16, 16, 6>;
-using V1 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 3, 0, 1, 16, 16, 6>;
-using V2 = SCfg<FGK_MOD_FREQOFF, 1536, 64, 6, 0, 1, 8, 8, 8, 3>;
+/* (16,16,6) with 128 threads: R16 stages use 96 of them, R6 stages two
+ * butterflies per thread. V0-V2 ping-pong (one butterfly in registers at a
+ * time, so 6-12 transforms per CTA fit); V3 in-place with direct loads; V4
+ * in-place with bulk-copy input. */
+using V0 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 6, 0, 2, 16, 16, 6>;
+using V1 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 7, 1, 2, 16, 16, 6>;
+using V2 = SCfg<FGK_MOD_FREQOFF, 1536, 64, 7, 1, 2, 16, 12, 8>;
 using V3 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 4, 0, 0, 16, 16, 6>;
-using V4 = SCfg<FGK_MOD_FREQOFF, 1536, 32, 12, 0, 0, 16, 12, 8>;
+using V4 = SCfg<FGK_MOD_FREQOFF, 1536, 128, 4, 0, 1, 16, 16, 6>;
 
 int static_entries_1536(const StaticEntry **out)
 {
