@@ -51,10 +51,12 @@ struct fftset_fft {
 	fgk_plan                        vp[FS_MAX_VAR]; /* their plans (chain of the variant) */
 	uint32_t                        vops[FS_MAX_VAR]; /* ops each variant implements (1 << op) */
 	int                             sel[FGK_OP_COUNT]; /* chosen variant per op, -1 = generic */
+	int                             fourstep; /* 1: sizes beyond shared memory, two HBM passes */
+	fgk_plan4                       p4;
 	void                           *dmem;  /* one device block for all tables */
 };
 
-#define FS_NSTAGE 3 /* staging buffers: input, output, kernel */
+#define FS_NSTAGE 4 /* staging buffers: input, output, kernel, four-step work */
 
 struct fs_impl {
 	cudaStream_t       stream;
@@ -190,6 +192,124 @@ static size_t fs_align(size_t x)
 	return (x + 255) & ~(size_t)255;
 }
 
+/* Plans beyond the shared-memory limit: four-step (two HBM passes). */
+static int fs_build_fourstep(struct fs_impl *fs, struct fftset_fft *f)
+{
+	fgk_plan4 *p = &f->p4;
+	const unsigned L = f->lfft;
+	const uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
+	size_t n1, n2, nhi, off[10], total, i;
+	float *h = NULL;
+	char *d = NULL;
+	int32_t *kidx = NULL;
+	unsigned lanes = 0;
+	cudaError_t e;
+	int rc = FFTSET_E_NOMEM;
+
+	if (fgk_plan_fourstep(p, L, modulation, fs->max_smem))
+		return FFTSET_E_UNSUPPORTED;
+	f->fourstep = 1;
+	f->nvar = 0;
+	for (i = 0; i < FGK_OP_COUNT; i++)
+		f->sel[i] = -1;
+	n1 = fgk_chain_twiddles(&p->c1, NULL);
+	n2 = fgk_chain_twiddles(&p->c2, NULL);
+	nhi = (L + 4095) / 4096;
+	/* float2 counts: tw1, tw2, thi, tlo, m1, m2, n1, n2; then kidx (int32) and the plan copy */
+	{
+		const size_t cnt[8] = {n1 ? n1 : 1, n2 ? n2 : 1, nhi, 4096, p->L1, p->L2, p->L1, p->L2};
+		total = fs_align(sizeof(fgk_plan4));
+		for (i = 0; i < 8; i++) {
+			off[i] = total;
+			total += fs_align(cnt[i] * 2 * sizeof(float));
+		}
+		off[8] = total;
+		total += fs_align(sizeof(int32_t) * L);
+	}
+	h = (float *)malloc(sizeof(float) * 2 * (n1 + n2 + nhi + 4096 + 2 * (size_t)p->L1 + 2 * (size_t)p->L2 + 2));
+	kidx = (int32_t *)malloc(sizeof(int32_t) * L);
+	if (!h || !kidx)
+		goto out;
+	if (fsl_kernel_offsets(f->modulator->freq_offset_real, L, fs->layout_vw, kidx, &lanes)) {
+		rc = FFTSET_E_INVALID;
+		goto out;
+	}
+	f->lanes = lanes;
+	if ((e = cudaMalloc((void **)&d, total)) != cudaSuccess) {
+		cudaGetLastError();
+		goto out;
+	}
+	{
+		float *w = h;
+		float *tw1 = w, *tw2, *thi, *tlo, *m1, *m2, *q1, *q2;
+		size_t k;
+		fgk_chain_twiddles(&p->c1, tw1);
+		tw2 = tw1 + 2 * (n1 ? n1 : 1);
+		fgk_chain_twiddles(&p->c2, tw2);
+		thi = tw2 + 2 * (n2 ? n2 : 1);
+		tlo = thi + 2 * nhi;
+		m1 = tlo + 2 * 4096;
+		m2 = m1 + 2 * (size_t)p->L1;
+		q1 = m2 + 2 * (size_t)p->L2;
+		q2 = q1 + 2 * (size_t)p->L1;
+		for (k = 0; k < nhi; k++) {
+			double a = -2.0 * M_PI * (double)(k * 4096) / (double)L;
+			thi[2 * k] = (float)cos(a);
+			thi[2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < 4096; k++) {
+			double a = -2.0 * M_PI * (double)k / (double)L;
+			tlo[2 * k] = (float)cos(a);
+			tlo[2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < p->L1; k++) {
+			double a = -M_PI * (double)k / (2.0 * p->L1), b = -M_PI * (double)k / (2.0 * (double)L);
+			m1[2 * k] = (float)cos(a);
+			m1[2 * k + 1] = (float)sin(a);
+			q1[2 * k] = (float)cos(b);
+			q1[2 * k + 1] = (float)sin(b);
+		}
+		for (k = 0; k < p->L2; k++) {
+			double a = -M_PI * (double)k / (2.0 * (double)L), b = -M_PI * (double)k / (2.0 * p->L2);
+			m2[2 * k] = (float)cos(a);
+			m2[2 * k + 1] = (float)sin(a);
+			q2[2 * k] = (float)cos(b);
+			q2[2 * k + 1] = (float)sin(b);
+		}
+		{
+			float *srcs[8] = {tw1, tw2, thi, tlo, m1, m2, q1, q2};
+			const size_t cnt[8] = {n1, n2, nhi, 4096, p->L1, p->L2, p->L1, p->L2};
+			const void **dst[8] = {&p->tw1, &p->tw2, &p->thi, &p->tlo, &p->m1, &p->m2, &p->n1, &p->n2};
+			for (k = 0; k < 8; k++) {
+				*dst[k] = d + off[k];
+				if (cnt[k] &&
+				    (e = cudaMemcpy(d + off[k], srcs[k], cnt[k] * 2 * sizeof(float), cudaMemcpyHostToDevice)) !=
+				        cudaSuccess)
+					goto cuda_fail;
+			}
+		}
+	}
+	p->dev = (const fgk_plan4 *)d;
+	if ((e = cudaMemcpy(d + off[8], kidx, sizeof(int32_t) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	    (e = cudaMemcpy(d, p, sizeof(fgk_plan4), cudaMemcpyHostToDevice)) != cudaSuccess)
+		goto cuda_fail;
+	f->rp.kidx = (const int32_t *)(d + off[8]);
+	f->rp.kvw = lanes;
+	f->rp.L = L;
+	f->rp.modulation = modulation;
+	f->dmem = d;
+	rc = FFTSET_OK;
+	goto out;
+cuda_fail:
+	fs_cuda(fs, e);
+	cudaFree(d);
+	rc = FFTSET_E_CUDA;
+out:
+	free(h);
+	free(kidx);
+	return rc;
+}
+
 /* Build the device tables of a plan: the generic resident plan (chain from
  * the GPU planner) plus one twiddle table per compile-time variant (each
  * variant has its own chain); modulation factors and the kernel-layout index
@@ -207,7 +327,7 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 	cudaError_t e;
 
 	if (fgk_plan_resident(rp, L, modulation, fs->max_smem, NULL, 0))
-		return FFTSET_E_UNSUPPORTED;
+		return fs_build_fourstep(fs, f);
 	ntw = fgk_plan_twiddles(rp, NULL);
 	nvar = fgk_static_count(modulation, L);
 	if (nvar > FS_MAX_VAR)
@@ -422,9 +542,25 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
 }
 
+static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);
+
 static int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
                      unsigned count, size_t in_stride, size_t out_stride)
 {
+	if (f->fourstep) {
+		/* two passes through a work buffer of 2L floats per transform (the
+		 * library's own scratch: work_buf of the reference API may be host
+		 * memory or too small for batches) */
+		struct fs_impl *fs = f->fs;
+		const size_t nf = 2 * (size_t)f->lfft;
+		int rc;
+		if (op != FGK_OP_FORWARD && op != FGK_OP_INVERSE)
+			return -FFTSET_E_UNSUPPORTED;
+		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0)
+			return -rc;
+		return fgk_launch_fourstep(&f->p4, op, out, in, (float *)fs->stage[3], count, in_stride ? in_stride : nf,
+		                           out_stride ? out_stride : nf, nf, fs->stream);
+	}
 	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
 	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride);
 }
@@ -459,6 +595,8 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 
 	if (fs_is_device_ptr(in) && fs_is_device_ptr(out) && (kern == NULL || fs_is_device_ptr(kern))) {
 		rc = fs_launch(f, op, out, in, kern, count, in_stride, out_stride);
+		if (rc < 0)
+			return fs_latch(fs, -rc, 0);
 		if (rc)
 			return fs_latch(fs, FFTSET_E_CUDA, rc);
 		if (fs->blocking) {
@@ -499,7 +637,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 	}
 	rc = fs_launch(f, op, dout, din, dkern, count, in_stride, out_stride);
 	if (rc) {
-		rc = fs_latch(fs, FFTSET_E_CUDA, rc);
+		rc = rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
 		goto done;
 	}
 	if (dout != out) {

@@ -59,6 +59,23 @@ typedef struct fgk_plan {
 	const struct fgk_plan *dev; /* device copy of this struct (kernels index its chains) */
 } fgk_plan;
 
+/* Plan of a four-step transform L = L1 * L2 (fgk_fourstep.cu). Pass 1 runs
+ * L2 column DFTs of length L1, pass 2 L1 row DFTs of length L2; a CTA holds
+ * 1 << lshift transforms lane-interleaved (mirrored passes need >= 2). */
+typedef struct fgk_plan4 {
+	uint32_t  L1, L2, modulation;
+	uint32_t  lshift1, lshift2;
+	uint32_t  threads1, threads2;
+	uint32_t  slots1, slots2;   /* shared float2 slots per CTA */
+	uint32_t  emax1, emax2;
+	fgk_chain c1, c2;
+	const void *tw1, *tw2;      /* chain twiddles */
+	const void *thi, *tlo;      /* w_L^m = thi[m >> 12] * tlo[m & 4095] */
+	const void *m1, *m2;        /* e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2L)}: input modulation */
+	const void *n1, *n2;        /* e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2)}: output modulation */
+	const struct fgk_plan4 *dev;
+} fgk_plan4;
+
 /* Host-side planning helpers implemented in fgk_plan.c */
 int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
 /* forced_radices: NULL, or the chain a static kernel was compiled for */
@@ -66,11 +83,19 @@ int  fgk_plan_resident(fgk_plan *p, uint32_t L, uint32_t modulation, uint32_t ma
                        const uint32_t *forced_radices, uint32_t forced_n);
 /* Number of float2 twiddles both chains of p need; fills them when tw != NULL. */
 size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2);
+/* Four-step planning: fills sizes, lanes, threads and chains (not the
+ * pointers). Returns -1 when L has no two-factor split the kernels take. */
+int    fgk_plan_fourstep(fgk_plan4 *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes);
+/* twiddles of one chain (the chain's tw_off fields are set) */
+size_t fgk_chain_twiddles(fgk_chain *c, void *tw_host_float2);
 
 /* Launchers implemented in fgk_kernels.cu. All return 0 or a cudaError_t. */
 int fgk_launch_resident(const fgk_plan *p, int op, float *out, const float *in, const float *kern,
                         uint32_t count, size_t in_stride, size_t out_stride, void *stream);
 uint32_t fgk_max_resident_L(void);
+/* two launches (pass 1, pass 2); work: count transforms of 2L floats at work_stride */
+int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, float *work, uint32_t count,
+                        size_t in_stride, size_t out_stride, size_t work_stride, void *stream);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -237,3 +237,90 @@ size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2)
 	size_t off = chain_twiddles(&p->fwd, tw, 0);
 	return chain_twiddles(&p->inv, tw, off);
 }
+
+size_t fgk_chain_twiddles(fgk_chain *c, void *tw_host_float2)
+{
+	return chain_twiddles(c, (float *)tw_host_float2, 0);
+}
+
+/* Threads a lane-interleaved pass needs: every stage's NL * Lp / R
+ * butterflies over at most `cap` threads, emax / R of them per thread. */
+static uint32_t pass_threads(const uint32_t *rad, uint32_t n, uint32_t Lp, uint32_t nl, uint32_t emax)
+{
+	uint32_t s, T = 32;
+	for (s = 0; s < n; s++) {
+		uint32_t items = Lp / rad[s] * nl, b = bmax(rad[s], emax);
+		uint32_t need = (items + b - 1) / b;
+		if (need > T)
+			T = need;
+	}
+	return (T + 31) & ~31u;
+}
+
+static int plan_pass(uint32_t Lp, int mirror, uint32_t max_smem, fgk_chain *ch, uint32_t *lshift, uint32_t *threads,
+                     uint32_t *slots, uint32_t *emax_out)
+{
+	uint32_t rad[FGK_MAX_STAGES], n, ls, emax;
+	if (fgk_plan_chain(Lp, rad, &n))
+		return -1;
+	/* widest lane count (<= 16) whose tile fits half the shared memory (two
+	 * CTAs per SM) and whose stages fit 512 threads; below 4 lanes the HBM
+	 * segments get narrower than a 32-byte sector, so 4 lanes may take the
+	 * whole shared memory */
+	for (ls = 4;; ls--) {
+		uint32_t nl = 1u << ls, sl = Lp * nl + (Lp * nl) / 16 + 1;
+		int ok = 0;
+		if ((size_t)sl * 8 <= max_smem / 2 || (ls <= 2 && (size_t)sl * 8 <= max_smem)) {
+			for (emax = 16; emax <= 32; emax *= 2) {
+				uint32_t T = pass_threads(rad, n, Lp, nl, emax);
+				if (T <= 512) {
+					*threads = T;
+					*emax_out = emax;
+					*slots = sl;
+					*lshift = ls;
+					ok = 1;
+					break;
+				}
+			}
+		}
+		if (ok)
+			break;
+		if (ls == (mirror ? 1u : 0u))
+			return -1;
+	}
+	fill_chain(ch, rad, n, Lp, *threads);
+	return 0;
+}
+
+int fgk_plan_fourstep(fgk_plan4 *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes)
+{
+	uint32_t a, b, c, L1, best1 = 0;
+	double bestd = 1e30;
+	memset(p, 0, sizeof(*p));
+	if (factor235(L, &a, &b, &c))
+		return -1;
+	/* most balanced split L1 * L2 (both at least 2) */
+	for (L1 = 2; (uint64_t)L1 * L1 <= (uint64_t)L * 4 && L1 < L; L1++) {
+		double d;
+		if (L % L1)
+			continue;
+		d = fabs(log((double)L1) - log((double)(L / L1)));
+		if (d < bestd) {
+			bestd = d;
+			best1 = L1;
+		}
+	}
+	if (!best1)
+		return -1;
+	p->L1 = best1;
+	p->L2 = L / best1;
+	p->modulation = modulation;
+	/* FREQ_OFFSET_REAL pairs mirror columns (inverse pass 1) and mirror rows
+	 * (forward pass 2) inside a CTA */
+	if (plan_pass(p->L1, modulation == FGK_MOD_FREQOFF, max_smem_bytes, &p->c1, &p->lshift1, &p->threads1,
+	              &p->slots1, &p->emax1) ||
+	    plan_pass(p->L2, modulation == FGK_MOD_FREQOFF, max_smem_bytes, &p->c2, &p->lshift2, &p->threads2,
+	              &p->slots2, &p->emax2))
+		return -1;
+	return 0;
+}

@@ -352,3 +352,61 @@ def test_autotune_picks_a_working_kernel(fftset_lib, gpu_set):
     y = torch.empty(512, 3072, device="cuda")
     f.conv_batch(y, dev(x), K)
     assert O.rel_l2(host(y), O.conv64(1, x, h)) <= tol(1, 1536)
+
+
+FOURSTEP = [32768, 36864, 46656, 59049, 65536, 131072, 393216]
+
+
+@pytest.mark.parametrize("mod", [0, 1])
+@pytest.mark.parametrize("L", FOURSTEP)
+def test_fourstep_sizes_against_fp64(gpu_set, mod, L):
+    """Sizes beyond the shared-memory limit (two HBM passes), including odd
+    ones (59049 = 3^10) whose FREQ_OFFSET_REAL mirror pairing has a
+    self-mirrored middle row: forward and inverse vs FP64, batched and in
+    place."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    assert f is not None
+    rng = np.random.default_rng(L + mod)
+    B = 2
+    x = rng.standard_normal((B, 2 * L)).astype(np.float32)
+    X = torch.empty(B, 2 * L, device="cuda")
+    f.forward_batch(X, dev(x))
+    Xh = host(X)
+    assert O.rel_l2(Xh, O.forward64(mod, x)) <= tol(mod, L)
+    r = torch.empty_like(X)
+    f.inverse_batch(r, X)
+    assert O.rel_l2(host(r), O.inverse64(mod, Xh)) <= tol(mod, L)
+    buf = dev(x[0])
+    f.forward(buf, buf)
+    assert O.rel_l2(host(buf), Xh[0]) <= 1e-6
+
+
+def test_fourstep_large_single(gpu_set):
+    """The 15,728,640-bin FREQ_OFFSET_REAL transform: forward against FP64
+    (error per bin band) and the forward/inverse round trip."""
+    import torch
+    L = 15728640
+    f = gpu_set.create_fft(1, L)
+    assert f is not None
+    rng = np.random.default_rng(6)
+    n = np.arange(2 * L)
+    freqs = rng.uniform(0, L, 64)
+    amps = rng.uniform(0.01, 1, 64)
+    phases = rng.uniform(0, 2 * np.pi, 64)
+    x = np.zeros(2 * L)
+    for fr, a, ph in zip(freqs, amps, phases):
+        x += a * np.cos(np.pi * fr * n / L + ph)
+    x = (x + rng.normal(0, 1e-3, 2 * L)).astype(np.float32)
+    X = torch.empty(2 * L, device="cuda")
+    f.forward(X, dev(x))
+    Xh = host(X).astype(np.float64)
+    want = O.freqoff_forward64(x)
+    assert O.rel_l2(Xh, want) <= tol(1, L)
+    bands = np.array_split(np.arange(L), 8)
+    for b in bands:
+        sl = np.concatenate([2 * b, 2 * b + 1])
+        assert O.rel_l2(Xh[sl], want[sl]) <= 10 * tol(1, L)
+    r = torch.empty(2 * L, device="cuda")
+    f.inverse(r, X)
+    assert O.rel_l2(host(r) / L, x) <= tol(1, L)
