@@ -554,12 +554,10 @@ static int fs_launch(const struct fftset_fft *f, int op, float *out, const float
 		struct fs_impl *fs = f->fs;
 		const size_t nf = 2 * (size_t)f->lfft;
 		int rc;
-		if (op != FGK_OP_FORWARD && op != FGK_OP_INVERSE)
-			return -FFTSET_E_UNSUPPORTED;
 		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0)
 			return -rc;
-		return fgk_launch_fourstep(&f->p4, op, out, in, (float *)fs->stage[3], count, in_stride ? in_stride : nf,
-		                           out_stride ? out_stride : nf, nf, fs->stream);
+		return fgk_launch_fourstep(&f->p4, op, out, in, kern, f->rp.kidx, (int)f->rp.kvw, (float *)fs->stage[3],
+		                           count, in_stride ? in_stride : nf, out_stride ? out_stride : nf, nf, fs->stream);
 	}
 	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
 	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride);

@@ -93,9 +93,12 @@ size_t fgk_chain_twiddles(fgk_chain *c, void *tw_host_float2);
 int fgk_launch_resident(const fgk_plan *p, int op, float *out, const float *in, const float *kern,
                         uint32_t count, size_t in_stride, size_t out_stride, void *stream);
 uint32_t fgk_max_resident_L(void);
-/* two launches (pass 1, pass 2); work: count transforms of 2L floats at work_stride */
-int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, float *work, uint32_t count,
-                        size_t in_stride, size_t out_stride, size_t work_stride, void *stream);
+/* two launches per DFT (pass 1, pass 2; convolution: two DFTs); work: count
+ * transforms of 2L floats at work_stride; kern/kidx/kvw: the kernel buffer and
+ * its layout table (get_kernel, conv) */
+int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
+                        const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
+                        size_t out_stride, size_t work_stride, void *stream);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -30,6 +30,10 @@
 
 namespace fgk {
 
+/* pass-1 input modes and pass-2 output modes */
+enum { FGK4_IN_FORWARD = 0, FGK4_IN_INVERSE = 1, FGK4_IN_NATURAL = 2 };
+enum { FGK4_OUT_FORWARD = 0, FGK4_OUT_FINAL = 1, FGK4_OUT_KERNEL = 2, FGK4_OUT_PRODUCT = 3, FGK4_OUT_PRODUCT_CONJ = 4 };
+
 #define FGK4_RADIX_SWITCH(r, CALL)                                  \
 	switch (r) {                                                    \
 	case 2: { constexpr int R_ = 2; CALL; } break;                  \
@@ -144,7 +148,7 @@ __host__ __device__ __forceinline__ uint32_t lane_groups(uint32_t len, int nl, b
 
 /* Pass 1: columns. */
 template <int EMAX>
-__global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int op, const float *in, float2 *work,
+__global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int mode, const float *in, float2 *work,
                                                           uint32_t count, size_t in_stride, size_t work_stride)
 {
 	extern __shared__ float2 smem[];
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 	const uint32_t L1 = p.L1, L2 = p.L2;
 	const uint64_t L = (uint64_t)L1 * L2;
 	const bool freq = p.modulation == FGK_MOD_FREQOFF;
-	const bool inverse = op == FGK_OP_INVERSE;
+	const bool inverse = mode == FGK4_IN_INVERSE;
 	const bool mirror = freq && inverse;
 	const uint32_t groups = lane_groups(L2, t.nl, mirror);
 	const uint64_t tr = blockIdx.x / groups;
@@ -177,7 +181,9 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 		float2 v = make_float2(0.f, 0.f);
 		if (valid) {
 			const uint64_t n = (uint64_t)L2 * n1 + n2;
-			if (!inverse) {
+			if (mode == FGK4_IN_NATURAL) {
+				v = __ldcs(reinterpret_cast<const float2 *>(x) + n);
+			} else if (!inverse) {
 				if (freq) {
 					const float2 m = cmul(__ldg((const float2 *)p.m1 + n1), __ldg((const float2 *)p.m2 + n2));
 					v = cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), m);
@@ -207,8 +213,10 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 
 /* Pass 2: rows. */
 template <int EMAX>
-__global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int op, const float2 *work, float *out,
-                                                          uint32_t count, size_t work_stride, size_t out_stride)
+__global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int mode, const float2 *work, float *out,
+                                                          uint32_t count, size_t work_stride, size_t out_stride,
+                                                          const float *__restrict__ kern, const int32_t *__restrict__ kidx,
+                                                          int kvw)
 {
 	extern __shared__ float2 smem[];
 	const fgk_plan4 *dp = p.dev;
@@ -222,7 +230,7 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 	const uint32_t L1 = p.L1, L2 = p.L2;
 	const uint64_t L = (uint64_t)L1 * L2;
 	const bool freq = p.modulation == FGK_MOD_FREQOFF;
-	const bool forward = op == FGK_OP_FORWARD;
+	const bool forward = mode == FGK4_OUT_FORWARD;
 	const bool mirror = freq && forward;
 	const uint32_t groups = lane_groups(L1, t.nl, mirror);
 	const uint64_t tr = blockIdx.x / groups;
@@ -269,7 +277,17 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 			continue;
 		}
 		const float2 v = t.ld(k2, lane);
-		if (forward) {
+		if (mode == FGK4_OUT_KERNEL) {
+			/* spectrum bin m into the reference's kernel-buffer layout */
+			const int ko = __ldg(kidx + m);
+			o[ko] = v.x;
+			o[ko + kvw] = v.y;
+		} else if (mode == FGK4_OUT_PRODUCT || mode == FGK4_OUT_PRODUCT_CONJ) {
+			/* conj(W K) (or conj(W conj K)), natural order, for the second half of a convolution */
+			const int ko = __ldg(kidx + m);
+			const float2 k = make_float2(__ldg(kern + ko), __ldg(kern + ko + kvw));
+			__stcs(reinterpret_cast<float2 *>(o) + m, conjf2(mode == FGK4_OUT_PRODUCT ? cmul(v, k) : cmulc(v, k)));
+		} else if (forward) {
 			__stcs(reinterpret_cast<float2 *>(o) + m, v);
 		} else if (freq) {
 			const float2 md = cmul(__ldg((const float2 *)p.n1 + k1), __ldg((const float2 *)p.n2 + k2));
@@ -284,19 +302,15 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 
 } /* namespace fgk */
 
-extern "C" int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, float *work,
-                                   uint32_t count, size_t in_stride, size_t out_stride, size_t work_stride,
-                                   void *stream)
+static int launch_pass(const fgk_plan4 *p, int in_mode, int out_mode, float *out, const float *in, float *work,
+                       uint32_t count, size_t in_stride, size_t out_stride, size_t work_stride, const float *kern,
+                       const int32_t *kidx, int kvw, cudaStream_t stream)
 {
 	using namespace fgk;
-	if (count == 0)
-		return 0;
-	if (op != FGK_OP_FORWARD && op != FGK_OP_INVERSE)
-		return (int)cudaErrorInvalidValue;
 	const bool freq = p->modulation == FGK_MOD_FREQOFF;
 	const int nl1 = 1 << p->lshift1, nl2 = 1 << p->lshift2;
-	const uint32_t g1 = lane_groups(p->L2, nl1, freq && op == FGK_OP_INVERSE);
-	const uint32_t g2 = lane_groups(p->L1, nl2, freq && op == FGK_OP_FORWARD);
+	const uint32_t g1 = lane_groups(p->L2, nl1, freq && in_mode == FGK4_IN_INVERSE);
+	const uint32_t g2 = lane_groups(p->L1, nl2, freq && out_mode == FGK4_OUT_FORWARD);
 	const size_t sm1 = (size_t)p->slots1 * sizeof(float2), sm2 = (size_t)p->slots2 * sizeof(float2);
 	auto k1 = p->emax1 > 16 ? fourstep_pass1<32> : fourstep_pass1<16>;
 	auto k2 = p->emax2 > 16 ? fourstep_pass2<32> : fourstep_pass2<16>;
@@ -308,11 +322,45 @@ extern "C" int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const
 	const uint64_t b1 = (uint64_t)g1 * count, b2 = (uint64_t)g2 * count;
 	if (b1 > 0x7fffffffull || b2 > 0x7fffffffull)
 		return (int)cudaErrorInvalidValue;
-	k1<<<(unsigned)b1, p->threads1, sm1, (cudaStream_t)stream>>>(*p, op, in, reinterpret_cast<float2 *>(work), count,
-	                                                                in_stride, work_stride / 2);
+	k1<<<(unsigned)b1, p->threads1, sm1, stream>>>(*p, in_mode, in, reinterpret_cast<float2 *>(work), count, in_stride,
+	                                                 work_stride / 2);
 	if ((e = cudaGetLastError()) != cudaSuccess)
 		return (int)e;
-	k2<<<(unsigned)b2, p->threads2, sm2, (cudaStream_t)stream>>>(*p, op, reinterpret_cast<const float2 *>(work), out,
-	                                                                count, work_stride / 2, out_stride);
+	k2<<<(unsigned)b2, p->threads2, sm2, stream>>>(*p, out_mode, reinterpret_cast<const float2 *>(work), out, count,
+	                                                 work_stride / 2, out_stride, kern, kidx, kvw);
 	return (int)cudaGetLastError();
+}
+
+extern "C" int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
+                                   const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
+                                   size_t out_stride, size_t work_stride, void *stream)
+{
+	using namespace fgk;
+	cudaStream_t s = (cudaStream_t)stream;
+	if (count == 0)
+		return 0;
+	switch (op) {
+	case FGK_OP_FORWARD:
+		return launch_pass(p, FGK4_IN_FORWARD, FGK4_OUT_FORWARD, out, in, work, count, in_stride, out_stride,
+		                   work_stride, kern, kidx, kvw, s);
+	case FGK_OP_INVERSE:
+		return launch_pass(p, FGK4_IN_INVERSE, FGK4_OUT_FINAL, out, in, work, count, in_stride, out_stride,
+		                   work_stride, kern, kidx, kvw, s);
+	case FGK_OP_KERNEL:
+		return launch_pass(p, FGK4_IN_FORWARD, FGK4_OUT_KERNEL, out, in, work, count, in_stride, out_stride,
+		                   work_stride, kern, kidx, kvw, s);
+	case FGK_OP_CONV:
+	case FGK_OP_CORR: {
+		/* DFT, conj(W K) in natural order into out, then a forward DFT of
+		 * that (= conj of the inverse) with the final step: four passes */
+		int rc = launch_pass(p, FGK4_IN_FORWARD, op == FGK_OP_CONV ? FGK4_OUT_PRODUCT : FGK4_OUT_PRODUCT_CONJ, out,
+		                     in, work, count, in_stride, out_stride, work_stride, kern, kidx, kvw, s);
+		if (rc)
+			return rc;
+		return launch_pass(p, FGK4_IN_NATURAL, FGK4_OUT_FINAL, out, out, work, count, out_stride, out_stride,
+		                   work_stride, kern, kidx, kvw, s);
+	}
+	default:
+		return (int)cudaErrorInvalidValue;
+	}
 }

@@ -380,6 +380,15 @@ def test_fourstep_sizes_against_fp64(gpu_set, mod, L):
     buf = dev(x[0])
     f.forward(buf, buf)
     assert O.rel_l2(host(buf), Xh[0]) <= 1e-6
+    # kernel buffer in the reference layout, and the convolution (in place)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    want_k = O.kernel_from_spectrum(mod, O.spectrum64(mod, h), 4)
+    assert O.rel_l2(host(K), want_k) <= tol(mod, L)
+    y = dev(x)
+    f.conv_batch(y, y, K)
+    assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
 
 
 def test_fourstep_large_single(gpu_set):
