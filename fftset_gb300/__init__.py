@@ -72,6 +72,13 @@ _decl("fftset_fft_autotune", C.c_int, [_vp, C.c_int, _u, C.POINTER(C.c_float)])
 
 OP_FORWARD, OP_INVERSE, OP_GET_KERNEL, OP_CONV, OP_CORR = range(5)
 
+_decl("fftset_ragged_create", _vp, [_P, _vp, C.c_int, _u, C.POINTER(_u), C.POINTER(_sz), C.POINTER(_sz)])
+_decl("fftset_ragged_execute", C.c_int, [_vp, _vp, _vp])
+_decl("fftset_ragged_set_graph", C.c_int, [_vp, C.c_int])
+_decl("fftset_ragged_bytes", C.c_double, [_vp])
+_decl("fftset_ragged_persistent_items", _u, [_vp])
+_decl("fftset_ragged_destroy", None, [_vp])
+
 MODULATION_COMPLEX = _vp.in_dll(_lib, "FFTSET_MODULATION_COMPLEX").value
 MODULATION_FREQ_OFFSET_REAL = _vp.in_dll(_lib, "FFTSET_MODULATION_FREQ_OFFSET_REAL").value
 COMPLEX, FREQ_OFFSET_REAL = 0, 1
@@ -288,3 +295,52 @@ class Fft:
 
     def conv_batch(self, out, inp, kern):
         return self._batch(_lib.fftset_fft_conv_batch, out, inp, kern)
+
+
+class Ragged:
+    """A ragged batch (fftset_ragged_*): item i has bins[i] complex bins,
+    input at in_offsets[i] and output at out_offsets[i] floats from the base
+    tensors given to execute()."""
+
+    def __init__(self, owner: FftSet, modulation, op: int, bins, in_offsets, out_offsets):
+        n = len(bins)
+        self.owner = owner
+        b = (_u * n)(*bins)
+        io = (_sz * n)(*in_offsets)
+        oo = (_sz * n)(*out_offsets)
+        self.h = _lib.fftset_ragged_create(owner.handle, _mod_ptr(modulation), op, n, b, io, oo)
+        if not self.h:
+            owner.check()
+            raise FftsetError("fftset_ragged_create failed")
+        self.n = n
+
+    @property
+    def bytes(self) -> float:
+        return float(_lib.fftset_ragged_bytes(self.h))
+
+    @property
+    def persistent_items(self) -> int:
+        return int(_lib.fftset_ragged_persistent_items(self.h))
+
+    def set_graph(self, enable: bool):
+        _lib.fftset_ragged_set_graph(self.h, 1 if enable else 0)
+
+    def execute(self, out, inp):
+        import torch
+        self.owner.set_stream(torch.cuda.current_stream())
+        rc = _lib.fftset_ragged_execute(self.h, _ptr(out), _ptr(inp))
+        if rc:
+            self.owner.check()
+            raise FftsetError(error_string(rc))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.fftset_ragged_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

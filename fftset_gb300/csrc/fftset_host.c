@@ -19,6 +19,7 @@
 #include <cuda_runtime_api.h>
 
 #include "fftset.h"
+#include "fftset_internal.h"
 #include "fftset_layout.h"
 #include "fgk.h"
 
@@ -26,62 +27,22 @@
 #define M_PI 3.14159265358979323846
 #endif
 
-struct fftset_modulation {
-	int         freq_offset_real;
-	const char *name;
-};
-
 static const struct fftset_modulation FS_MOD_FREQOFF = {1, "FREQ_OFFSET_REAL"};
 static const struct fftset_modulation FS_MOD_COMPLEX = {0, "COMPLEX"};
 const struct fftset_modulation *FFTSET_MODULATION_FREQ_OFFSET_REAL = &FS_MOD_FREQOFF;
 const struct fftset_modulation *FFTSET_MODULATION_COMPLEX = &FS_MOD_COMPLEX;
-
-struct fs_impl;
-
-#define FS_MAX_VAR 8
-
-struct fftset_fft {
-	unsigned                        lfft;
-	const struct fftset_modulation *modulator;
-	struct fftset_fft              *next;
-	struct fs_impl                 *fs;
-	unsigned                        lanes; /* kernel-buffer lane width */
-	fgk_plan                        rp;    /* generic resident plan (device pointers inside) */
-	int                             nvar;  /* compile-time kernel variants for this size */
-	fgk_plan                        vp[FS_MAX_VAR]; /* their plans (chain of the variant) */
-	uint32_t                        vops[FS_MAX_VAR]; /* ops each variant implements (1 << op) */
-	int                             sel[FGK_OP_COUNT]; /* chosen variant per op, -1 = generic */
-	int                             fourstep; /* 1: sizes beyond shared memory, two HBM passes */
-	fgk_plan4                       p4;
-	void                           *dmem;  /* one device block for all tables */
-};
-
-#define FS_NSTAGE 4 /* staging buffers: input, output, kernel, four-step work */
-
-struct fs_impl {
-	cudaStream_t       stream;
-	cudaStream_t       own_stream;
-	int                blocking;
-	unsigned           layout_vw;
-	int                err;
-	int                cuda_err;
-	int                device;
-	unsigned           max_smem;
-	int                num_sms;
-	struct fftset_fft *first;
-	pthread_mutex_t    lock;
-	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
-	int               *dev_flag;
-	void              *stage[FS_NSTAGE];
-	size_t             stage_bytes[FS_NSTAGE];
-};
 
 static struct fs_impl *fs_of(const struct fftset *fc)
 {
 	return fc ? (struct fs_impl *)fc->impl : NULL;
 }
 
-static int fs_latch(struct fs_impl *fs, int code, int cuda_err)
+struct fs_impl *fs_impl_of(struct fftset *fc)
+{
+	return fs_of(fc);
+}
+
+int fs_latch(struct fs_impl *fs, int code, int cuda_err)
 {
 	if (fs && code && !fs->err) {
 		fs->err = code;
@@ -90,7 +51,7 @@ static int fs_latch(struct fs_impl *fs, int code, int cuda_err)
 	return code;
 }
 
-static int fs_cuda(struct fs_impl *fs, cudaError_t e)
+int fs_cuda(struct fs_impl *fs, cudaError_t e)
 {
 	if (e == cudaSuccess)
 		return FFTSET_OK;
@@ -160,6 +121,7 @@ void fftset_destroy(struct fftset *fc)
 	for (p = fs->first; p != NULL; p = n) {
 		n = p->next;
 		cudaFree(p->dmem);
+		cudaFree(p->dmem4);
 		free(p);
 	}
 	for (i = 0; i < FS_NSTAGE; i++)
@@ -192,8 +154,10 @@ static size_t fs_align(size_t x)
 	return (x + 255) & ~(size_t)255;
 }
 
-/* Plans beyond the shared-memory limit: four-step (two HBM passes). */
-static int fs_build_fourstep(struct fs_impl *fs, struct fftset_fft *f)
+/* Four-step tables (two HBM passes) into their own device allocation:
+ * the plan of sizes beyond the shared-memory limit, and on demand for
+ * resident sizes that a ragged batch runs through the four-step passes. */
+int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 {
 	fgk_plan4 *p = &f->p4;
 	const unsigned L = f->lfft;
@@ -206,12 +170,10 @@ static int fs_build_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 	cudaError_t e;
 	int rc = FFTSET_E_NOMEM;
 
+	if (f->dmem4)
+		return FFTSET_OK;
 	if (fgk_plan_fourstep(p, L, modulation, fs->max_smem))
 		return FFTSET_E_UNSUPPORTED;
-	f->fourstep = 1;
-	f->nvar = 0;
-	for (i = 0; i < FGK_OP_COUNT; i++)
-		f->sel[i] = -1;
 	n1 = fgk_chain_twiddles(&p->c1, NULL);
 	n2 = fgk_chain_twiddles(&p->c2, NULL);
 	nhi = (L + 4095) / 4096;
@@ -293,11 +255,8 @@ static int fs_build_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 	if ((e = cudaMemcpy(d + off[8], kidx, sizeof(int32_t) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
 	    (e = cudaMemcpy(d, p, sizeof(fgk_plan4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		goto cuda_fail;
-	f->rp.kidx = (const int32_t *)(d + off[8]);
-	f->rp.kvw = lanes;
-	f->rp.L = L;
-	f->rp.modulation = modulation;
-	f->dmem = d;
+	f->kidx4 = (const int32_t *)(d + off[8]);
+	f->dmem4 = d;
 	rc = FFTSET_OK;
 	goto out;
 cuda_fail:
@@ -326,8 +285,13 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 	int rc = FFTSET_E_NOMEM, v, op, nvar;
 	cudaError_t e;
 
-	if (fgk_plan_resident(rp, L, modulation, fs->max_smem, NULL, 0))
-		return fs_build_fourstep(fs, f);
+	if (fgk_plan_resident(rp, L, modulation, fs->max_smem, NULL, 0)) {
+		f->fourstep = 1;
+		f->nvar = 0;
+		for (v = 0; v < FGK_OP_COUNT; v++)
+			f->sel[v] = -1;
+		return fs_ensure_fourstep(fs, f);
+	}
 	ntw = fgk_plan_twiddles(rp, NULL);
 	nvar = fgk_static_count(modulation, L);
 	if (nvar > FS_MAX_VAR)
@@ -473,7 +437,7 @@ const struct fftset_fft *fftset_create_fft(struct fftset *fc, const struct fftse
 /* ------------------------------------------------------------------------
  * Execution */
 
-static int fs_is_device_ptr(const void *ptr)
+int fs_is_device_ptr(const void *ptr)
 {
 	struct cudaPointerAttributes a;
 	if (ptr == NULL)
@@ -507,7 +471,7 @@ static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 }
 
 /* A kernel whose bounded wait gave up wrote 1 to the mapped flag. */
-static int fs_check_flag(struct fs_impl *fs)
+int fs_check_flag(struct fs_impl *fs)
 {
 	if (*(volatile int *)fs->host_flag) {
 		*(volatile int *)fs->host_flag = 0;
@@ -556,7 +520,7 @@ static int fs_launch(const struct fftset_fft *f, int op, float *out, const float
 		int rc;
 		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0)
 			return -rc;
-		return fgk_launch_fourstep(&f->p4, op, out, in, kern, f->rp.kidx, (int)f->rp.kvw, (float *)fs->stage[3],
+		return fgk_launch_fourstep(&f->p4, op, out, in, kern, f->kidx4, (int)f->lanes, (float *)fs->stage[3],
 		                           count, in_stride ? in_stride : nf, out_stride ? out_stride : nf, nf, fs->stream);
 	}
 	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;

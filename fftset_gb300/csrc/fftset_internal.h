@@ -1,0 +1,70 @@
+/* Internal structures of the host layer, shared by fftset_host.c and
+ * fftset_ragged.c. Not part of the public interface. */
+#ifndef FFTSET_INTERNAL_H
+#define FFTSET_INTERNAL_H
+
+#include <pthread.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#include "fftset.h"
+#include "fgk.h"
+
+struct fftset_modulation {
+	int         freq_offset_real;
+	const char *name;
+};
+
+struct fs_impl;
+
+#define FS_MAX_VAR 8
+
+struct fftset_fft {
+	unsigned                        lfft;
+	const struct fftset_modulation *modulator;
+	struct fftset_fft              *next;
+	struct fs_impl                 *fs;
+	unsigned                        lanes; /* kernel-buffer lane width */
+	fgk_plan                        rp;    /* generic resident plan (device pointers inside) */
+	int                             nvar;  /* compile-time kernel variants for this size */
+	fgk_plan                        vp[FS_MAX_VAR]; /* their plans (chain of the variant) */
+	uint32_t                        vops[FS_MAX_VAR]; /* ops each variant implements (1 << op) */
+	int                             sel[FGK_OP_COUNT]; /* chosen variant per op, -1 = generic */
+	int                             fourstep; /* 1: sizes beyond shared memory, two HBM passes */
+	fgk_plan4                       p4;    /* four-step plan (when dmem4 != NULL) */
+	void                           *dmem4; /* its device tables */
+	const int32_t                  *kidx4; /* kernel-layout table in dmem4 */
+	void                           *dmem;  /* one device block for all tables */
+};
+
+#define FS_NSTAGE 4 /* staging buffers: input, output, kernel, four-step work */
+
+struct fs_impl {
+	cudaStream_t       stream;
+	cudaStream_t       own_stream;
+	int                blocking;
+	unsigned           layout_vw;
+	int                err;
+	int                cuda_err;
+	int                device;
+	unsigned           max_smem;
+	int                num_sms;
+	struct fftset_fft *first;
+	pthread_mutex_t    lock;
+	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
+	int               *dev_flag;
+	void              *stage[FS_NSTAGE];
+	size_t             stage_bytes[FS_NSTAGE];
+};
+
+
+/* helpers implemented in fftset_host.c */
+int  fs_latch(struct fs_impl *fs, int code, int cuda_err);
+int  fs_cuda(struct fs_impl *fs, cudaError_t e);
+int  fs_is_device_ptr(const void *ptr);
+int  fs_check_flag(struct fs_impl *fs);
+/* four-step tables for a plan (built on demand for resident-size plans too) */
+int  fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f);
+struct fs_impl *fs_impl_of(struct fftset *fc);
+
+#endif

@@ -76,6 +76,17 @@ typedef struct fgk_plan4 {
 	const struct fgk_plan4 *dev;
 } fgk_plan4;
 
+/* Ragged batches: item offsets (floats, from the batch's base pointers) and
+ * chunks of up to n same-size items run side by side in one CTA, tg threads
+ * each (fgk_ragged.cu). */
+typedef struct fgk_rg_item {
+	uint64_t in_off, out_off;
+} fgk_rg_item;
+
+typedef struct fgk_rg_chunk {
+	uint32_t plan, first, n, tg;
+} fgk_rg_chunk;
+
 /* Host-side planning helpers implemented in fgk_plan.c */
 int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
 /* forced_radices: NULL, or the chain a static kernel was compiled for */
@@ -99,6 +110,16 @@ uint32_t fgk_max_resident_L(void);
 int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
                         const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
                         size_t out_stride, size_t work_stride, void *stream);
+/* the same for `count` transforms at item offsets (forward / inverse) */
+int fgk_launch_fourstep_items(const fgk_plan4 *p, int op, float *out_base, const float *in_base,
+                              const fgk_rg_item *items_dev, float *work, uint32_t count, size_t work_stride,
+                              void *stream);
+/* one persistent launch over all chunks (fgk_ragged.cu); counter_dev: one
+ * int of device scratch, reset by the launcher */
+int    fgk_launch_ragged(const fgk_plan *plans_dev, const fgk_rg_chunk *chunks_dev, uint32_t nchunks,
+                         const fgk_rg_item *items_dev, int *counter_dev, int op, const float *in_base,
+                         float *out_base, int num_sms, void *stream);
+size_t fgk_ragged_smem_bytes(void);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -1,0 +1,190 @@
+/* Ragged batches: many transforms of different sizes in one persistent
+ * launch.
+ *
+ * The host groups the items by size (largest first) into chunks of up to G
+ * same-size items; CTAs (512 threads, 227 KB of shared memory, one per SM)
+ * claim chunks from an atomic counter. A chunk's items run side by side, one
+ * group of threads each, as ping-pong Stockham chains in shared memory: each
+ * stage reads one buffer and writes the other, one butterfly per thread at a
+ * time (only one radix worth of values is live, so the runtime-dispatched
+ * radix costs no spills), one barrier per stage. Plans (chain, twiddles,
+ * modulation factors) are the fftset's own plans for each size, so all sizes
+ * share the fftset's twiddle tables. Items too large for two shared buffers
+ * go through the four-step passes (fgk_fourstep.cu) with an item list. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fgk.h"
+#include "fgk_codelets.cuh"
+
+namespace fgk {
+
+#define FGKR_RADIX_SWITCH(r, CALL)                                  \
+	switch (r) {                                                    \
+	case 2: { constexpr int R_ = 2; CALL; } break;                  \
+	case 3: { constexpr int R_ = 3; CALL; } break;                  \
+	case 4: { constexpr int R_ = 4; CALL; } break;                  \
+	case 5: { constexpr int R_ = 5; CALL; } break;                  \
+	case 6: { constexpr int R_ = 6; CALL; } break;                  \
+	case 8: { constexpr int R_ = 8; CALL; } break;                  \
+	case 10: { constexpr int R_ = 10; CALL; } break;                \
+	case 12: { constexpr int R_ = 12; CALL; } break;                \
+	case 15: { constexpr int R_ = 15; CALL; } break;                \
+	default: { constexpr int R_ = 16; CALL; } break;                \
+	}
+
+__device__ __forceinline__ int rslot(int i) { return i + (i >> 4); }
+
+/* one stage, src -> dst, this thread's butterflies j = tid, tid + T, ... */
+template <int R>
+__device__ __forceinline__ void rg_stage(const float2 *src, float2 *dst, int L, int ns, const float2 *__restrict__ tw,
+                                         int tid, int T)
+{
+	const int nbf = L / R;
+	for (int j = tid; j < nbf; j += T) {
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = src[rslot(j + p * nbf)];
+		const int k = j % ns;
+		if (ns > 1) {
+			const float2 *t = tw + k * (R - 1);
+#pragma unroll
+			for (int p = 1; p < R; p++)
+				v[p] = cmul(v[p], __ldg(t + p - 1));
+		}
+		Radix<R>::run(v);
+		const int base = (j - k) * R + k;
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			dst[rslot(base + q * ns)] = v[q];
+	}
+}
+
+__global__ void __launch_bounds__(512, 1)
+    ragged_kernel(const fgk_plan *__restrict__ plans, const fgk_rg_chunk *__restrict__ chunks, uint32_t nchunks,
+                  const fgk_rg_item *__restrict__ items, int *counter, int op, const float *in_base, float *out_base)
+{
+	extern __shared__ float2 smem[];
+	__shared__ uint32_t cur;
+	for (;;) {
+		if (threadIdx.x == 0)
+			cur = (uint32_t)atomicAdd(counter, 1);
+		__syncthreads();
+		const uint32_t c = cur;
+		if (c >= nchunks)
+			break;
+		const fgk_rg_chunk ch = chunks[c];
+		const fgk_plan *pl = plans + ch.plan;
+		const int L = (int)pl->L;
+		const int n = (int)pl->fwd.nstages;
+		const bool freq = pl->modulation == FGK_MOD_FREQOFF;
+		const float2 *mod = (const float2 *)pl->modtw;
+		const float2 *tw = (const float2 *)pl->tw;
+		const int T = (int)ch.tg;
+		const int g = (int)threadIdx.x / T;
+		const int tid = (int)threadIdx.x - g * T;
+		const bool active = g < (int)ch.n;
+		const int slots = L + L / 16 + 1;
+		float2 *buf0 = smem + (size_t)(active ? g : 0) * 2 * slots;
+		float2 *buf1 = buf0 + slots;
+		const fgk_rg_item it = active ? items[ch.first + g] : fgk_rg_item{0, 0};
+		const float *x = in_base + it.in_off;
+		float *y = out_base + it.out_off;
+
+		/* prologue: the sequence to transform, natural order */
+		if (active) {
+			if (op != FGK_OP_INVERSE) {
+				if (freq) {
+					for (int i = tid; i < L; i += T)
+						buf0[rslot(i)] = cmul(make_float2(__ldcs(x + i), -__ldcs(x + L + i)), __ldg(mod + i));
+				} else {
+					const float2 *x2 = reinterpret_cast<const float2 *>(x);
+					for (int i = tid; i < L; i += T)
+						buf0[rslot(i)] = __ldcs(x2 + i);
+				}
+			} else {
+				const float2 *X = reinterpret_cast<const float2 *>(x);
+				if (freq) {
+					const int half = L >> 1;
+					for (int m = tid; m < half; m += T) {
+						buf0[rslot(m)] = conjf2(__ldcs(X + 2 * m));
+						buf0[rslot(L - 1 - m)] = __ldcs(X + 2 * m + 1);
+					}
+					if ((L & 1) && tid == 0)
+						buf0[rslot(half)] = conjf2(__ldcs(X + L - 1));
+				} else {
+					for (int i = tid; i < L; i += T)
+						buf0[rslot(i)] = conjf2(__ldcs(X + i));
+				}
+			}
+		}
+		__syncthreads();
+		float2 *src = buf0, *dst = buf1;
+		for (int s = 0; s < n; s++) {
+			const fgk_stage st = pl->fwd.st[s];
+			if (active)
+				FGKR_RADIX_SWITCH(st.radix, (rg_stage<R_>(src, dst, L, (int)st.ns, tw + st.tw_off, tid, T)));
+			__syncthreads();
+			float2 *t = src;
+			src = dst;
+			dst = t;
+		}
+		/* epilogue from src */
+		if (active) {
+			if (op == FGK_OP_INVERSE) {
+				if (freq) {
+					for (int i = tid; i < L; i += T) {
+						const float2 r = cmul(src[rslot(i)], __ldg(mod + i));
+						__stcs(y + i, r.x);
+						__stcs(y + L + i, r.y);
+					}
+				} else {
+					float2 *y2 = reinterpret_cast<float2 *>(y);
+					for (int i = tid; i < L; i += T)
+						__stcs(y2 + i, conjf2(src[rslot(i)]));
+				}
+			} else if (freq) {
+				float2 *y2 = reinterpret_cast<float2 *>(y);
+				const int half = L >> 1;
+				for (int m = tid; m < half; m += T) {
+					__stcs(y2 + 2 * m, src[rslot(m)]);
+					__stcs(y2 + 2 * m + 1, conjf2(src[rslot(L - 1 - m)]));
+				}
+				if ((L & 1) && tid == 0)
+					__stcs(y2 + L - 1, src[rslot(half)]);
+			} else {
+				float2 *y2 = reinterpret_cast<float2 *>(y);
+				for (int i = tid; i < L; i += T)
+					__stcs(y2 + i, src[rslot(i)]);
+			}
+		}
+		__syncthreads(); /* buffers and `cur` are reused by the next chunk */
+	}
+}
+
+} /* namespace fgk */
+
+extern "C" size_t fgk_ragged_smem_bytes(void)
+{
+	return 232448 - 1024; /* the opt-in limit less room for static shared memory */
+}
+
+extern "C" int fgk_launch_ragged(const fgk_plan *plans_dev, const fgk_rg_chunk *chunks_dev, uint32_t nchunks,
+                                 const fgk_rg_item *items_dev, int *counter_dev, int op, const float *in_base,
+                                 float *out_base, int num_sms, void *stream)
+{
+	using namespace fgk;
+	const size_t smem = fgk_ragged_smem_bytes();
+	cudaError_t e;
+	if (nchunks == 0)
+		return 0;
+	if ((e = cudaFuncSetAttribute((const void *)ragged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                              (int)smem)) != cudaSuccess)
+		return (int)e;
+	if ((e = cudaMemsetAsync(counter_dev, 0, sizeof(int), (cudaStream_t)stream)) != cudaSuccess)
+		return (int)e;
+	const uint32_t grid = (uint32_t)num_sms < nchunks ? (uint32_t)num_sms : nchunks;
+	ragged_kernel<<<grid, 512, smem, (cudaStream_t)stream>>>(plans_dev, chunks_dev, nchunks, items_dev, counter_dev, op,
+	                                                         in_base, out_base);
+	return (int)cudaGetLastError();
+}

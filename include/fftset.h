@@ -158,6 +158,24 @@ int fftset_fft_variant(const struct fftset_fft *fft, int op);
 int fftset_fft_set_variant(const struct fftset_fft *fft, int op, int variant);
 int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, float *best_ms);
 
+/* Ragged batches: n transforms of different sizes (bins[i] complex bins,
+ * same modulation, op FFTSET_OP_FORWARD or FFTSET_OP_INVERSE), item i read
+ * from input_base + in_offsets[i] and written to output_base + out_offsets[i]
+ * (offsets in floats, even; device buffers). All sizes share the fftset's
+ * plans and twiddles. Sizes whose two shared-memory buffers fit one CTA run
+ * in one persistent launch; larger ones run the four-step passes; the
+ * sequence is captured in a CUDA graph on the first execute (again when the
+ * base pointers change) and replayed. */
+struct fftset_ragged;
+struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftset_modulation *modulation, int op,
+                                           unsigned n, const unsigned *bins, const size_t *in_offsets,
+                                           const size_t *out_offsets);
+int      fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base);
+int      fftset_ragged_set_graph(struct fftset_ragged *rb, int enable);
+double   fftset_ragged_bytes(const struct fftset_ragged *rb);  /* one read + one write of every item */
+unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb);
+void     fftset_ragged_destroy(struct fftset_ragged *rb);
+
 /* Private Parts
  * ---------------------------------------------------------------------------
  * Don't touch them. */

@@ -1,0 +1,84 @@
+"""Ragged batches through the C ABI: many sizes in one submission (persistent
+launch for resident sizes, four-step passes for the rest, CUDA graph
+replay), every item against FP64."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def draw_sizes(n, seed, lo=60, hi=65536):
+    """Log-uniform in [lo, hi], snapped (in log space) to the nearest
+    2^a 3^b 5^{0,1} size."""
+    valid = np.array(O.valid_sizes(lo, hi))
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(np.log(lo), np.log(hi), n)
+    idx = np.abs(np.log(valid)[None, :] - u[:, None]).argmin(1)
+    return valid[idx]
+
+
+def layout(sizes, gap=2):
+    offs, o = [], 0
+    for L in sizes:
+        offs.append(o)
+        o += 2 * int(L) + gap
+    return offs, o
+
+
+@pytest.mark.parametrize("mod", [0, 1])
+@pytest.mark.parametrize("graph", [True, False])
+def test_ragged_forward_inverse(fftset_lib, gpu_set, mod, graph):
+    import torch
+    sizes = draw_sizes(240, seed=4 + mod)
+    sizes[:3] = [65536, 59049, 60]          # largest, odd four-step, smallest
+    offs, total = layout(sizes)
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, total).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    for op in (fftset_lib.OP_FORWARD, fftset_lib.OP_INVERSE):
+        rb = fftset_lib.Ragged(gpu_set, mod, op, [int(s) for s in sizes], offs, offs)
+        rb.set_graph(graph)
+        y = torch.full_like(xd, 3.0)
+        rb.execute(y, xd)
+        y1 = y.cpu().numpy()
+        rb.execute(y, xd)                       # replay
+        torch.cuda.synchronize()
+        assert np.array_equal(y.cpu().numpy(), y1)
+        assert 0 < rb.persistent_items < len(sizes)
+        for L, o in zip(sizes, offs):
+            L = int(L)
+            xi = x[o:o + 2 * L]
+            want = O.forward64(mod, xi) if op == fftset_lib.OP_FORWARD else O.inverse64(mod, xi)
+            assert O.rel_l2(y1[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (L, op)
+            assert np.all(y1[o + 2 * L:o + 2 * L + 2] == 3.0)
+        rb.close()
+
+
+def test_ragged_equals_single_calls(fftset_lib, gpu_set):
+    import torch
+    sizes = [1024, 60, 4096, 1536, 27000 // 27 * 27 if O.valid_size(27000) else 26244, 32768, 100]
+    sizes = [s for s in sizes if O.valid_size(s)]
+    offs, total = layout(sizes, gap=0)
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal(total).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    rb = fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, sizes, offs, offs)
+    y = torch.empty_like(xd)
+    rb.execute(y, xd)
+    torch.cuda.synchronize()
+    for L, o in zip(sizes, offs):
+        f = gpu_set.create_fft(0, L)
+        one = torch.empty(2 * L, device="cuda")
+        f.forward(one, xd[o:o + 2 * L])
+        torch.cuda.synchronize()
+        assert O.rel_l2(y[o:o + 2 * L].cpu().numpy(), one.cpu().numpy()) <= 1e-6, L
+    rb.close()
+
+
+def test_ragged_rejects_bad_input(fftset_lib, gpu_set):
+    with pytest.raises(fftset_lib.FftsetError):
+        fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 7], [0, 200], [0, 200])
+    with pytest.raises(fftset_lib.FftsetError):
+        fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64], [1], [0])
