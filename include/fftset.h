@@ -176,6 +176,31 @@ double   fftset_ragged_bytes(const struct fftset_ragged *rb);  /* one read + one
 unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb);
 void     fftset_ragged_destroy(struct fftset_ragged *rb);
 
+/* No counterpart in the reference. A batched call (op FFTSET_OP_*, the
+ * arguments of fftset_fft_*_batch) that allocates nothing, for callers that
+ * must not call cudaMalloc while they run: a real-time audio callback with a
+ * deadline every few milliseconds cannot block in the driver's allocator,
+ * and some hosts fix their device-memory budget up front. It is for sizes
+ * beyond the shared-memory limit, whose four-step passes need a work buffer
+ * of 2 * complex_bins floats per block; the regular calls grow the fftset's
+ * own work buffer with cudaMalloc, this one uses a fixed device array of
+ * FFTSET_FIXED_SCRATCH_FLOATS floats (32 MiB, held by every GPU that loads
+ * the library until the process exits).
+ * - count * 2 * complex_bins above FFTSET_FIXED_SCRATCH_FLOATS returns
+ *   FFTSET_E_INVALID; sizes that fit shared memory need no scratch and
+ *   return FFTSET_E_UNSUPPORTED (their fftset_fft_*_batch calls serve them).
+ * - Device buffers only; the fftset's device must be current.
+ * - The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ * - All calls in the process share the one array per device: calls that
+ *   overlap on the GPU (other streams, other fftsets, other threads) race
+ *   on it and give wrong results; serialise them. Nothing in it needs to
+ *   start at zero: the first pass writes all of it before the second reads. */
+#define FFTSET_FIXED_SCRATCH_FLOATS (8u << 20)
+int fftset_fft_execute_fixed_scratch(const struct fftset_fft *fft, int op, float *output_buf, size_t out_stride,
+                                     const float *input_buf, size_t in_stride, const float *kernel_buf,
+                                     unsigned count);
+
 /* Private Parts
  * ---------------------------------------------------------------------------
  * Don't touch them. */
