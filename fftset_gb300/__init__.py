@@ -78,6 +78,7 @@ _decl("fftset_ragged_set_graph", C.c_int, [_vp, C.c_int])
 _decl("fftset_ragged_bytes", C.c_double, [_vp])
 _decl("fftset_ragged_persistent_items", _u, [_vp])
 _decl("fftset_ragged_destroy", None, [_vp])
+_decl("fftset_fft_conv_adjoint_batch", C.c_int, [_vp, _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _u])
 
 MODULATION_COMPLEX = _vp.in_dll(_lib, "FFTSET_MODULATION_COMPLEX").value
 MODULATION_FREQ_OFFSET_REAL = _vp.in_dll(_lib, "FFTSET_MODULATION_FREQ_OFFSET_REAL").value
@@ -295,6 +296,22 @@ class Fft:
 
     def conv_batch(self, out, inp, kern):
         return self._batch(_lib.fftset_fft_conv_batch, out, inp, kern)
+
+    def conv_adjoint_batch(self, grad_input, grad_taps, grad_out, inp, kern):
+        """fftset_fft_conv_adjoint_batch: gradients of sum_b <grad_out_b, y_b>
+        for y_b = conv(inp_b, kern) with respect to inp ([count, stride],
+        may be None) and to the 2L taps that made kern (may be None)."""
+        self._sync_stream(grad_out, inp, kern, grad_input, grad_taps)
+        count = int(grad_out.shape[0]) if len(grad_out.shape) > 1 else 1
+        go = int(grad_out.shape[-1])
+        gi = int(grad_input.shape[-1]) if grad_input is not None else 0
+        ins = int(inp.shape[-1]) if inp is not None else 0
+        rc = _lib.fftset_fft_conv_adjoint_batch(self.handle, _ptr(grad_input), gi, _ptr(grad_taps), _ptr(grad_out),
+                                                go, _ptr(inp), ins, _ptr(kern), count)
+        if rc:
+            self.owner.check()
+            raise FftsetError(error_string(rc))
+        return grad_input, grad_taps
 
 
 class Ragged:

@@ -449,7 +449,7 @@ int fs_is_device_ptr(const void *ptr)
 	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
+int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 {
 	cudaError_t e;
 	if (fs->stage_bytes[slot] >= bytes)
@@ -506,9 +506,9 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
 }
 
-static int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);
 
-static int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
+
+int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
                      unsigned count, size_t in_stride, size_t out_stride)
 {
 	if (f->fourstep) {

@@ -37,7 +37,7 @@ struct fftset_fft {
 	void                           *dmem;  /* one device block for all tables */
 };
 
-#define FS_NSTAGE 4 /* staging buffers: input, output, kernel, four-step work */
+#define FS_NSTAGE 5 /* staging buffers: input, output, kernel, four-step work, adjoint scratch */
 
 struct fs_impl {
 	cudaStream_t       stream;
@@ -66,5 +66,11 @@ int  fs_check_flag(struct fs_impl *fs);
 /* four-step tables for a plan (built on demand for resident-size plans too) */
 int  fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f);
 struct fs_impl *fs_impl_of(struct fftset *fc);
+/* grows staging slot `slot` to at least `bytes` (cudaMalloc) */
+int  fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);
+/* runs op on `count` device-resident blocks on the fftset's stream;
+ * returns 0, a negative FFTSET_E_* code or a positive cudaError_t */
+int  fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern, unsigned count,
+               size_t in_stride, size_t out_stride);
 
 #endif

@@ -14,51 +14,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "fgk.h"
-#include "fgk_codelets.cuh"
+#include "fgk_pingpong.cuh"
 
 namespace fgk {
-
-#define FGKR_RADIX_SWITCH(r, CALL)                                  \
-	switch (r) {                                                    \
-	case 2: { constexpr int R_ = 2; CALL; } break;                  \
-	case 3: { constexpr int R_ = 3; CALL; } break;                  \
-	case 4: { constexpr int R_ = 4; CALL; } break;                  \
-	case 5: { constexpr int R_ = 5; CALL; } break;                  \
-	case 6: { constexpr int R_ = 6; CALL; } break;                  \
-	case 8: { constexpr int R_ = 8; CALL; } break;                  \
-	case 10: { constexpr int R_ = 10; CALL; } break;                \
-	case 12: { constexpr int R_ = 12; CALL; } break;                \
-	case 15: { constexpr int R_ = 15; CALL; } break;                \
-	default: { constexpr int R_ = 16; CALL; } break;                \
-	}
-
-__device__ __forceinline__ int rslot(int i) { return i + (i >> 4); }
-
-/* one stage, src -> dst, this thread's butterflies j = tid, tid + T, ... */
-template <int R>
-__device__ __forceinline__ void rg_stage(const float2 *src, float2 *dst, int L, int ns, const float2 *__restrict__ tw,
-                                         int tid, int T)
-{
-	const int nbf = L / R;
-	for (int j = tid; j < nbf; j += T) {
-		float2 v[R];
-#pragma unroll
-		for (int p = 0; p < R; p++)
-			v[p] = src[rslot(j + p * nbf)];
-		const int k = j % ns;
-		if (ns > 1) {
-			const float2 *t = tw + k * (R - 1);
-#pragma unroll
-			for (int p = 1; p < R; p++)
-				v[p] = cmul(v[p], __ldg(t + p - 1));
-		}
-		Radix<R>::run(v);
-		const int base = (j - k) * R + k;
-#pragma unroll
-		for (int q = 0; q < R; q++)
-			dst[rslot(base + q * ns)] = v[q];
-	}
-}
 
 __global__ void __launch_bounds__(512, 1)
     ragged_kernel(const fgk_plan *__restrict__ plans, const fgk_rg_chunk *__restrict__ chunks, uint32_t nchunks,
@@ -76,15 +34,13 @@ __global__ void __launch_bounds__(512, 1)
 		const fgk_rg_chunk ch = chunks[c];
 		const fgk_plan *pl = plans + ch.plan;
 		const int L = (int)pl->L;
-		const int n = (int)pl->fwd.nstages;
 		const bool freq = pl->modulation == FGK_MOD_FREQOFF;
 		const float2 *mod = (const float2 *)pl->modtw;
-		const float2 *tw = (const float2 *)pl->tw;
 		const int T = (int)ch.tg;
 		const int g = (int)threadIdx.x / T;
 		const int tid = (int)threadIdx.x - g * T;
 		const bool active = g < (int)ch.n;
-		const int slots = L + L / 16 + 1;
+		const int slots = rslots(L);
 		float2 *buf0 = smem + (size_t)(active ? g : 0) * 2 * slots;
 		float2 *buf1 = buf0 + slots;
 		const fgk_rg_item it = active ? items[ch.first + g] : fgk_rg_item{0, 0};
@@ -119,16 +75,7 @@ __global__ void __launch_bounds__(512, 1)
 			}
 		}
 		__syncthreads();
-		float2 *src = buf0, *dst = buf1;
-		for (int s = 0; s < n; s++) {
-			const fgk_stage st = pl->fwd.st[s];
-			if (active)
-				FGKR_RADIX_SWITCH(st.radix, (rg_stage<R_>(src, dst, L, (int)st.ns, tw + st.tw_off, tid, T)));
-			__syncthreads();
-			float2 *t = src;
-			src = dst;
-			dst = t;
-		}
+		const float2 *src = rg_chain(pl, buf0, buf1, active, tid, T, [] { __syncthreads(); });
 		/* epilogue from src */
 		if (active) {
 			if (op == FGK_OP_INVERSE) {

@@ -176,6 +176,21 @@ double   fftset_ragged_bytes(const struct fftset_ragged *rb);  /* one read + one
 unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb);
 void     fftset_ragged_destroy(struct fftset_ragged *rb);
 
+/* Adjoint of fftset_fft_conv (the reference has only the forward,
+ * src/fftset_vec.c:1161-1220). For count blocks y_b = conv(x_b, K) with
+ * K = fftset_fft_conv_get_kernel(h) and upstream gradients g_b (grad_output,
+ * strides in floats like the batched calls):
+ *   grad_input_b = conv of g_b with the conjugated kernel spectrum, i.e.
+ *                  complex_bins times the negacyclic (FREQ_OFFSET_REAL) or
+ *                  cyclic (COMPLEX) cross-correlation of g_b with h;
+ *   grad_taps    = sum over b of complex_bins times the cross-correlation of
+ *                  g_b with x_b: the gradient with respect to the 2L taps h.
+ * Either output may be NULL. Device buffers only. For FREQ_OFFSET_REAL these
+ * are the gradients of the real loss sum_b <g_b, y_b>. */
+int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_input, size_t gi_stride,
+                                  float *grad_taps, const float *grad_output, size_t go_stride,
+                                  const float *input_buf, size_t in_stride, const float *kernel_buf, unsigned count);
+
 /* No counterpart in the reference. A batched call (op FFTSET_OP_*, the
  * arguments of fftset_fft_*_batch) that allocates nothing, for callers that
  * must not call cudaMalloc while they run: a real-time audio callback with a

@@ -188,6 +188,43 @@ def conv64(modulation, x, h):
     return negacyclic_conv64(x, h) if modulation == MOD_FREQ_OFFSET_REAL else complex_conv64(x, h)
 
 
+def negacyclic_reverse(h: np.ndarray) -> np.ndarray:
+    """h'[0] = h[0], h'[k] = -h[N-k]: the negacyclic time reversal, whose
+    half-bin-offset spectrum is conj(H). Convolving with h' correlates with
+    h, which is how the gradient of a FREQ_OFFSET_REAL convolution is built
+    from the reference's own convolution (src/fftset_vec.c:1161-1220)."""
+    h = np.asarray(h)
+    return np.concatenate([h[..., :1], -h[..., :0:-1]], axis=-1)
+
+
+def conj_reverse_complex(hi: np.ndarray) -> np.ndarray:
+    """h*[k] = conj(h[-k mod L]) for interleaved complex h (spectrum conj(H)):
+    the COMPLEX counterpart of negacyclic_reverse."""
+    hi = np.asarray(hi)
+    h = hi[..., 0::2] + 1j * hi[..., 1::2]
+    r = np.conj(np.concatenate([h[..., :1], h[..., :0:-1]], axis=-1))
+    out = np.empty(hi.shape, np.float64)
+    out[..., 0::2] = r.real
+    out[..., 1::2] = r.imag
+    return out
+
+
+def reverse(modulation, h):
+    return negacyclic_reverse(h) if modulation == MOD_FREQ_OFFSET_REAL else conj_reverse_complex(h)
+
+
+def conv_adjoint64(modulation, x, h, g):
+    """FP64 adjoint of the batched convolution y_b = conv64(x_b, h) for
+    upstream gradients g_b: (dx, dh) with dx_b = conv64(g_b, reverse(h)) and
+    dh = sum_b conv64(g_b, reverse(x_b)); for FREQ_OFFSET_REAL the gradients
+    of the loss sum_b <g_b, y_b>."""
+    x = np.atleast_2d(np.asarray(x, np.float64))
+    g = np.atleast_2d(np.asarray(g, np.float64))
+    dx = conv64(modulation, g, reverse(modulation, np.asarray(h, np.float64))[None, :])
+    dh = conv64(modulation, g, reverse(modulation, x)).sum(axis=0)
+    return dx, dh
+
+
 def rel_l2(a, b) -> float:
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)

@@ -3,6 +3,7 @@ reference (tests/golden, made by tests/golden/make_golden.py), the
 reference's own known-answer tests (app_fftset_test/fftset_test.c) and the
 FP64 definitions. CPU only."""
 import hashlib
+import os
 
 import numpy as np
 import pytest
@@ -119,3 +120,49 @@ def test_recommend_conv_length_reference_values(golden_layouts):
     """Checked against the product implementation in test_abi.py."""
     rec = golden_layouts["recommend"]
     assert rec.shape[1] == 3 and len(rec) > 50
+
+
+def test_fp64_adjoint_against_finite_differences():
+    """oracle.conv_adjoint64 is the gradient of sum_b <g_b, conv64(x_b, h)>
+    (both modulations; COMPLEX data as interleaved reals)."""
+    rng = np.random.default_rng(3)
+    for mod in (0, 1):
+        L = 10
+        x, g = rng.standard_normal((2, 2 * L)), rng.standard_normal((2, 2 * L))
+        h = rng.standard_normal(2 * L)
+        dx, dh = O.conv_adjoint64(mod, x, h, g)
+
+        def loss(xx, hh):
+            return float(np.sum(g * O.conv64(mod, xx, hh[None, :])))
+
+        eps = 1e-6
+        fx = np.zeros_like(x)
+        fh = np.zeros_like(h)
+        for b in range(2):
+            for n in range(2 * L):
+                e = np.zeros_like(x)
+                e[b, n] = eps
+                fx[b, n] = (loss(x + e, h) - loss(x - e, h)) / (2 * eps)
+        for n in range(2 * L):
+            e = np.zeros_like(h)
+            e[n] = eps
+            fh[n] = (loss(x, h + e) - loss(x, h - e)) / (2 * eps)
+        assert O.rel_l2(dx, fx) <= 1e-7
+        assert O.rel_l2(dh, fh) <= 1e-7
+
+
+def test_fp64_adjoint_against_reference_gradients():
+    """The FP64 adjoint against gradients built from the unmodified
+    reference's CPU convolution with time-reversed kernels
+    (tests/golden/ref_adjoint_vw4.npz)."""
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_adjoint_vw4.npz"))
+    keys = sorted({k.rsplit("_", 1)[0] for k in gold.files})
+    for key in keys:
+        mod, L = int(key.split("_")[0][1:]), int(key.split("_")[1][1:])
+        dx, dh = O.conv_adjoint64(mod, gold[key + "_x"], gold[key + "_h"], gold[key + "_g"])
+        assert O.rel_l2(gold[key + "_dx"], dx) <= O.tolerance(2 * L if mod else L), key
+        assert O.rel_l2(gold[key + "_dh"], dh) <= O.tolerance(2 * L if mod else L), key
+        # and the oracle's C restatement reproduces the reference gradient
+        P = O.PortPlan(mod, L, 4)
+        rx = P.conv(gold[key + "_g"], P.get_kernel(O.reverse(mod, gold[key + "_h"]).astype(np.float32)))
+        assert O.rel_l2(rx, gold[key + "_dx"]) <= O.tolerance(2 * L if mod else L), key
