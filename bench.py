@@ -132,6 +132,220 @@ def cpu_baseline(x, h, nthreads=None, reps=3):
             "seconds_per_step": best}
 
 
+# ---------------------------------------------------------------------------
+# The other workloads, reported beside the headline line (rank 0, N = 1).
+
+def _valid_size(n: int) -> bool:
+    for p in (2, 3):
+        while n % p == 0:
+            n //= p
+    if n % 5 == 0:
+        n //= 5
+    return n == 1
+
+
+def ragged_sizes(n: int, seed: int, lo: int = 60, hi: int = 65536) -> np.ndarray:
+    """Sizes drawn log-uniformly in [lo, hi] and snapped (in log space) to the
+    nearest 2^a 3^b 5^{0,1} size."""
+    valid = np.array([v for v in range(lo, hi + 1) if _valid_size(v)])
+    u = np.random.default_rng(seed).uniform(np.log(lo), np.log(hi), n)
+    return valid[np.abs(np.log(valid)[None, :] - u[:, None]).argmin(1)]
+
+
+def _events_ms(torch, fn, reps, stream):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def workload_percall_complex1024(fs, torch, peak):
+    """COMPLEX 1024 bins, 256 transforms: fftset_fft_forward then
+    fftset_fft_inverse on each, called one by one (the blocking drop-in
+    calls, device buffers); the same 256 transforms as two batched calls
+    beside it."""
+    from oracle import oracle as O
+    L, n = 1024, 256
+    S = fs.FftSet()
+    f = S.create_fft(fs.COMPLEX, L)
+    x_np = np.random.default_rng(1).uniform(-1, 1, (n, 2 * L)).astype(np.float32)
+    x = torch.from_numpy(x_np).cuda()
+    X = torch.empty_like(x)
+    r = torch.empty_like(x)
+    S.set_stream(torch.cuda.current_stream())
+    lib = fs.library()
+    xp = [x[i].data_ptr() for i in range(n)]
+    Xp = [X[i].data_ptr() for i in range(n)]
+    rp = [r[i].data_ptr() for i in range(n)]
+
+    def percall():
+        for i in range(n):
+            lib.fftset_fft_forward(f.handle, Xp[i], xp[i], None)
+            lib.fftset_fft_inverse(f.handle, rp[i], Xp[i], None)
+
+    percall()
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        percall()
+    torch.cuda.synchronize()
+    t_call = (time.perf_counter() - t0) / reps
+    S.check()
+    rel = O.rel_l2(X.cpu().numpy()[:16], O.complex_forward64(x_np[:16]))
+    rt = O.rel_l2(r.cpu().numpy() / L, x_np)
+    S.set_blocking(False)
+
+    def batched():
+        f.forward_batch(X, x)
+        f.inverse_batch(r, X)
+
+    batched()
+    t_batch = _events_ms(torch, batched, 50, torch.cuda.current_stream()) * 1e-3
+    S.close()
+    nbytes = n * 2 * 16 * L
+    return {"workload": "complex_L1024_x256_fwd_inv_per_call", "transforms_per_s": 2 * n / t_call,
+            "gbs": nbytes / t_call / 1e9, "us_per_call": t_call / (2 * n) * 1e6,
+            "batched_gbs": nbytes / t_batch / 1e9, "batched_transforms_per_s": 2 * n / t_batch,
+            "frac_of_peak_batched": nbytes / t_batch / 1e9 / peak,
+            "relL2_fwd_vs_fp64": rel, "relL2_roundtrip": rt, "tolerance": O.tolerance(L)}
+
+
+def workload_ragged(fs, torch, peak):
+    """20000 COMPLEX forward transforms, sizes log-uniform over the
+    2^a 3^b 5^{0,1} sizes in [60, 65536], one ragged submission replayed
+    from a CUDA graph; against the plain per-call drop-in on the same items."""
+    from oracle import oracle as O
+    sizes = [int(v) for v in ragged_sizes(20000, 4)]
+    offs, o = [], 0
+    for v in sizes:
+        offs.append(o)
+        o += 2 * v
+    x_np = np.random.default_rng(5).uniform(-1, 1, o).astype(np.float32)
+    x = torch.from_numpy(x_np).cuda()
+    y = torch.empty_like(x)
+    S = fs.FftSet()
+    S.set_stream(torch.cuda.current_stream())
+    rb = fs.Ragged(S, fs.COMPLEX, fs.OP_FORWARD, sizes, offs, offs)
+    S.set_blocking(False)
+    rb.execute(y, x)
+    rb.execute(y, x)
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, lambda: rb.execute(y, x), 10, torch.cuda.current_stream())
+    nbytes = rb.bytes
+    yh = y.cpu().numpy()
+    rng = np.random.default_rng(6)
+    chk = sorted(set(rng.integers(0, len(sizes), 48).tolist()) | {int(np.argmax(sizes)), int(np.argmin(sizes))})
+    worst = 0.0
+    for i in chk:
+        L, a = sizes[i], offs[i]
+        e = O.rel_l2(yh[a:a + 2 * L], O.complex_forward64(x_np[a:a + 2 * L])) / O.tolerance(L)
+        worst = max(worst, e)
+    # the plain per-call drop-in over the same items (blocking calls)
+    S.set_blocking(True)
+    lib = fs.library()
+    plans = {L: S.create_fft(fs.COMPLEX, L).handle for L in set(sizes)}
+    xb, yb = x.data_ptr(), y.data_ptr()
+    for i in range(min(200, len(sizes))):
+        lib.fftset_fft_forward(plans[sizes[i]], yb + 4 * offs[i], xb + 4 * offs[i], None)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for L, a in zip(sizes, offs):
+        lib.fftset_fft_forward(plans[L], yb + 4 * a, xb + 4 * a, None)
+    torch.cuda.synchronize()
+    t_call = time.perf_counter() - t0
+    S.check()
+    out = {"workload": "ragged_complex_fwd_20000_sizes_60_65536", "items": len(sizes),
+           "distinct_sizes": len(set(sizes)), "bytes": nbytes, "ms": ms, "gbs": nbytes / ms / 1e6,
+           "transforms_per_s": len(sizes) / ms * 1e3, "frac_of_peak": nbytes / ms / 1e6 / peak,
+           "persistent_items": rb.persistent_items, "percall_ms": t_call * 1e3,
+           "speedup_vs_percall": t_call * 1e3 / ms, "parity_worst_relL2_over_tol": worst,
+           "parity_items_checked": len(chk)}
+    rb.close()
+    S.close()
+    return out
+
+
+def workload_large(fs, torch, peak):
+    """FREQ_OFFSET_REAL forward + inverse at 15,728,640 bins (four-step: two
+    HBM passes per transform): 64 sinusoids + Gaussian noise 1e-3."""
+    L = 15728640
+    N = 2 * L
+    rng = np.random.default_rng(6)
+    n = torch.arange(N, device="cuda", dtype=torch.float64)
+    xd = torch.zeros(N, device="cuda", dtype=torch.float64)
+    for fr, a, ph in zip(rng.uniform(0, L, 64), rng.uniform(0.01, 1, 64), rng.uniform(0, 2 * np.pi, 64)):
+        xd += a * torch.cos(np.pi * fr * n / L + ph)
+    xd += torch.from_numpy(rng.normal(0, 1e-3, N)).cuda()
+    x = xd.float()
+    del n, xd
+    S = fs.FftSet()
+    S.set_stream(torch.cuda.current_stream())
+    f = S.create_fft(fs.FREQ_OFFSET_REAL, L)
+    X = torch.empty_like(x)
+    r = torch.empty_like(x)
+    S.set_blocking(False)
+
+    def pair():
+        f.forward(X, x)
+        f.inverse(r, X)
+
+    pair()
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, pair, 10, torch.cuda.current_stream())
+    rt = float(torch.linalg.norm(r / L - x) / torch.linalg.norm(x))
+    S.check()
+    S.close()
+    nbytes = 2 * 2 * N * 4
+    return {"workload": "freqoffsetreal_L15728640_fwd_inv", "ms_per_pair": ms, "gbs": nbytes / ms / 1e6,
+            "frac_of_peak": nbytes / ms / 1e6 / peak, "hbm_passes_per_transform": 2,
+            "relL2_roundtrip": rt, "tolerance": 2e-6 * np.log2(N)}
+
+
+def workload_adjoint(fs, torch, peak):
+    """Differentiable FREQ_OFFSET_REAL conv, 4096 bins, batch 2048: forward
+    conv, then the adjoint (dL/dx and dL/dtaps) for loss sum w*y."""
+    from oracle import oracle as O
+    L, B = 4096, 2048
+    N = 2 * L
+    x_np = np.random.default_rng(7).standard_normal((B, N)).astype(np.float32)
+    h_np = (np.random.default_rng(8).standard_normal(N) * np.exp(-np.arange(N) / 1000.0)).astype(np.float32)
+    w_np = np.random.default_rng(9).standard_normal((B, N)).astype(np.float32)
+    x, h, w = (torch.from_numpy(a).cuda() for a in (x_np, h_np, w_np))
+    S = fs.FftSet()
+    S.set_stream(torch.cuda.current_stream())
+    f = S.create_fft(fs.FREQ_OFFSET_REAL, L)
+    K = torch.empty_like(h)
+    f.conv_get_kernel(K, h)
+    y, dx, dh = torch.empty_like(x), torch.empty_like(x), torch.empty_like(h)
+    S.set_blocking(False)
+    st = torch.cuda.current_stream()
+    fwd = lambda: f.conv_batch(y, x, K)
+    bwd = lambda: f.conv_adjoint_batch(dx, dh, w, x, K)
+    fwd()
+    bwd()
+    torch.cuda.synchronize()
+    ms_f = _events_ms(torch, fwd, 20, st)
+    ms_b = _events_ms(torch, bwd, 20, st)
+    ms_dx = _events_ms(torch, lambda: f.conv_adjoint_batch(dx, None, w, x, K), 20, st)
+    ms_dh = _events_ms(torch, lambda: f.conv_adjoint_batch(None, dh, w, x, K), 20, st)
+    S.check()
+    wx, wh = O.conv_adjoint64(1, x_np[:64], h_np, w_np[:64])
+    rel_dx = O.rel_l2(dx[:64].cpu().numpy(), wx)
+    f.conv_adjoint_batch(None, dh, w[:64], x[:64], K)
+    rel_dh = O.rel_l2(dh.cpu().numpy(), wh)
+    S.close()
+    blk = B * N * 4
+    return {"workload": "freqoffsetreal_conv_adjoint_L4096_x2048", "fwd_ms": ms_f, "bwd_ms": ms_b,
+            "dx_ms": ms_dx, "dtaps_ms": ms_dh, "fwd_gbs": 2 * blk / ms_f / 1e6,
+            "dx_gbs": 2 * blk / ms_dx / 1e6, "dtaps_gbs": 2 * blk / ms_dh / 1e6,
+            "step_gbs": 6 * blk / (ms_f + ms_b) / 1e6, "frac_of_peak_step": 6 * blk / (ms_f + ms_b) / 1e6 / peak,
+            "relL2_dx_vs_fp64": rel_dx, "relL2_dtaps_vs_fp64_64blocks": rel_dh, "tolerance": O.tolerance(N)}
+
+
 def dist_setup(n_gpus):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -278,6 +492,17 @@ def run_gb300(args):
     achieved = BYTES_PER_STEP / (ms * 1e-3) / 1e9
     if rank == 0:
         cb = cpu_baseline(x_np, h_np) if world == 1 else None
+        others = {}
+        if world == 1 and not args.skip_workloads:
+            del x, y, xh, yh
+            torch.cuda.empty_cache()
+            for fn in (workload_percall_complex1024, workload_ragged, workload_large, workload_adjoint):
+                try:
+                    r = fn(fs, torch, peak)
+                    others[r.pop("workload")] = r
+                except Exception as ex:  # reported, never hidden
+                    others[fn.__name__] = {"error": repr(ex)}
+                torch.cuda.empty_cache()
         line = {
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -295,6 +520,7 @@ def run_gb300(args):
                     "parity_ok": bool(e2e_ok)},
             "gpu_launches": args.steps,
             "clocks": clocks,
+            "workloads": others,
         }
         print(json.dumps(line))
     S.close()
@@ -308,6 +534,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-workloads", action="store_true",
+                    help="only the headline workload (no per-call, ragged, large and adjoint lines)")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin the conv kernel variant (-1 generic) instead of autotuning")
     args = ap.parse_args()

@@ -2,14 +2,18 @@
  *
  * fftset_ragged_create plans every distinct size through the fftset's own
  * plan cache (fftset_create_fft, so all sizes share the fftset's twiddle
- * tables), sorts the items by size, and builds the device work list:
- *   - items whose two ping-pong buffers fit one CTA's shared memory go to one
- *     persistent launch (fgk_ragged.cu) as chunks of same-size items, largest
- *     first, claimed by CTAs from an atomic counter;
- *   - larger items run the four-step passes with an item list, by size, in
- *     sub-batches that share one work buffer.
- * fftset_ragged_execute records that sequence into a CUDA graph on first use
- * (and when the base pointers change) and replays the graph afterwards. */
+ * tables) and builds the task list of one persistent launch
+ * (fgk_tasks.cu), every task a tile of at most FGK_TASK_POINTS points:
+ *   - items up to FGK_TASK_POINTS bins: SMALL tasks of same-size items;
+ *   - larger items: their four-step split L = L1 L2, COLS tiles (columns
+ *     into the item's scratch) then ROWS tiles (rows into the output). The
+ *     ROWS tiles of item i are listed after the COLS tiles of item i + D,
+ *     D chosen so that a full grid of tasks separates them, so ROWS tiles
+ *     rarely wait.
+ * Big items come first (largest first), then the SMALL tasks (largest
+ * first), which balances the tail. fftset_ragged_execute records the launch
+ * into a CUDA graph on first use (and when the base pointers change) and
+ * replays the graph afterwards. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -19,28 +23,21 @@
 #include "fftset_internal.h"
 #include "fgk.h"
 
-#define FSR_WORK_CAP ((size_t)512 << 20) /* bytes of four-step work buffer */
-
-struct fsr_big {
-	const struct fftset_fft *f;
-	uint32_t                 first, count; /* into the device item array */
-};
+#define FSR_THREADS 256 /* threads of a task CTA */
 
 struct fftset_ragged {
 	struct fs_impl *fs;
 	int             op;
 	unsigned        n;
-	/* persistent part */
+	fgk_task       *tasks_dev;
+	uint32_t        ntasks;
 	fgk_plan       *plans_dev;
-	fgk_rg_chunk   *chunks_dev;
-	uint32_t        nchunks;
 	fgk_rg_item    *items_dev;
-	int            *counter_dev;
-	/* four-step part */
-	struct fsr_big *big;
+	fgk_big        *bigs_dev;
 	uint32_t        nbig;
-	float          *work;
-	size_t          work_floats;
+	uint32_t        nbig_items; /* items run as four-step tiles */
+	int            *counters_dev;
+	float          *scratch;
 	/* graph */
 	cudaStream_t    cap_stream;
 	cudaGraphExec_t exec;
@@ -63,8 +60,13 @@ static int fsr_cmp(const void *a, const void *b)
 	return x->idx < y->idx ? -1 : (x->idx > y->idx);
 }
 
-/* threads per item of a persistent chunk: enough for the widest stage, a
- * multiple of 32, at most the CTA */
+static uint32_t fsr_slots(uint32_t L)
+{
+	return L + L / 16 + 1;
+}
+
+/* threads per item of a SMALL task: enough for the widest stage, a multiple
+ * of 32, at most the CTA */
 static uint32_t fsr_item_threads(const fgk_plan *p)
 {
 	uint32_t s, w = 1;
@@ -74,7 +76,17 @@ static uint32_t fsr_item_threads(const fgk_plan *p)
 			w = nbf;
 	}
 	w = (w + 31) & ~31u;
-	return w > 512 ? 512 : w;
+	return w > FSR_THREADS ? FSR_THREADS : w;
+}
+
+/* log2 of the lanes of a tile of columns (rows) of length lp: as many as
+ * FGK_TASK_POINTS holds, no more than the `count` columns (rows) there are */
+static uint32_t fsr_lanes_log2(uint32_t lp, uint32_t count)
+{
+	uint32_t ls = 0;
+	while ((lp << (ls + 1)) <= FGK_TASK_POINTS && (1u << ls) < count)
+		ls++;
+	return ls;
 }
 
 void fftset_ragged_destroy(struct fftset_ragged *rb)
@@ -87,12 +99,12 @@ void fftset_ragged_destroy(struct fftset_ragged *rb)
 		cudaGraphExecDestroy(rb->exec);
 	if (rb->cap_stream)
 		cudaStreamDestroy(rb->cap_stream);
+	cudaFree(rb->tasks_dev);
 	cudaFree(rb->plans_dev);
-	cudaFree(rb->chunks_dev);
 	cudaFree(rb->items_dev);
-	cudaFree(rb->counter_dev);
-	cudaFree(rb->work);
-	free(rb->big);
+	cudaFree(rb->bigs_dev);
+	cudaFree(rb->counters_dev);
+	cudaFree(rb->scratch);
 	free(rb);
 }
 
@@ -104,10 +116,12 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	struct fftset_ragged *rb = NULL;
 	struct fsr_sort *order = NULL;
 	fgk_plan *plans = NULL;
-	fgk_rg_chunk *chunks = NULL;
 	fgk_rg_item *items = NULL;
-	unsigned i, j, nplans = 0, nchunks = 0, nitems = 0;
-	const size_t smem = fgk_ragged_smem_bytes();
+	fgk_big *bigs = NULL;
+	fgk_task *tasks = NULL;
+	unsigned i, j, nplans = 0, nitems = 0, nbig = 0, ntasks = 0, cap_tasks = 0;
+	size_t scratch_f2 = 0;
+	uint64_t total_cols = 0;
 	cudaError_t e;
 	int rc = FFTSET_E_NOMEM;
 
@@ -125,9 +139,9 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	rb = (struct fftset_ragged *)calloc(1, sizeof(*rb));
 	order = (struct fsr_sort *)malloc(sizeof(*order) * n);
 	plans = (fgk_plan *)calloc(n, sizeof(*plans));
-	chunks = (fgk_rg_chunk *)calloc(n, sizeof(*chunks));
 	items = (fgk_rg_item *)calloc(n, sizeof(*items));
-	if (!rb || !order || !plans || !chunks || !items)
+	bigs = (fgk_big *)calloc(n, sizeof(*bigs));
+	if (!rb || !order || !plans || !items || !bigs)
 		goto fail;
 	rb->fs = fs;
 	rb->op = op;
@@ -140,108 +154,117 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	}
 	qsort(order, n, sizeof(*order), fsr_cmp);
 
-	/* pass 1: persistent chunks for the sizes whose ping-pong buffers fit */
-	for (i = 0; i < n;) {
+	/* plans, items and big items; SMALL tasks are counted here, listed below */
+	for (i = 0; i < n; i = j) {
 		const unsigned L = order[i].bins;
-		const struct fftset_fft *f = fftset_create_fft(fc, modulation, L);
-		size_t per_item;
-		unsigned G, tg, cnt, m;
+		struct fftset_fft *f = (struct fftset_fft *)fftset_create_fft(fc, modulation, L);
 		for (j = i; j < n && order[j].bins == L; j++)
 			;
-		cnt = j - i;
 		if (!f) {
 			rc = FFTSET_E_INVALID;
 			goto fail;
 		}
-		per_item = 2 * ((size_t)L + L / 16 + 1) * 8;
-		if (f->fourstep || per_item > smem) {
-			i = j; /* second pass */
-			continue;
-		}
-		plans[nplans] = f->rp;
-		tg = fsr_item_threads(&f->rp);
-		G = 512 / tg;
-		if ((size_t)G * per_item > smem)
-			G = (unsigned)(smem / per_item);
-		for (; i < j; i += m) {
-			unsigned k;
-			m = j - i < G ? j - i : G;
-			chunks[nchunks].plan = nplans;
-			chunks[nchunks].first = nitems;
-			chunks[nchunks].n = m;
-			chunks[nchunks].tg = tg;
-			nchunks++;
-			for (k = 0; k < m; k++) {
-				items[nitems].in_off = in_offsets[order[i + k].idx];
-				items[nitems].out_off = out_offsets[order[i + k].idx];
-				nitems++;
-			}
-		}
-		nplans++;
-	}
-	/* pass 2: four-step items, grouped by size */
-	for (i = 0; i < n;) {
-		const unsigned L = order[i].bins;
-		struct fftset_fft *f = (struct fftset_fft *)fftset_create_fft(fc, modulation, L);
-		size_t per_item = 2 * ((size_t)L + L / 16 + 1) * 8;
-		for (j = i; j < n && order[j].bins == L; j++)
-			;
-		if (f->fourstep || per_item > smem) {
-			struct fsr_big *nb;
+		if (!f->fourstep && L <= FGK_TASK_POINTS) {
+			const uint32_t tg = fsr_item_threads(&f->rp);
+			uint32_t G = FSR_THREADS / tg;
+			if (G * fsr_slots(L) > fsr_slots(FGK_TASK_POINTS))
+				G = fsr_slots(FGK_TASK_POINTS) / fsr_slots(L);
+			plans[nplans] = f->rp;
+			cap_tasks += (j - i + G - 1) / G;
+			plans[nplans].threads = tg; /* reused below: threads per item */
+			plans[nplans].per_cta = G;  /* and items per task */
+			nplans++;
+		} else {
+			uint32_t L1, L2, k;
 			if ((rc = fs_ensure_fourstep(fs, f)) != 0)
 				goto fail;
-			nb = (struct fsr_big *)realloc(rb->big, sizeof(*nb) * (rb->nbig + 1));
-			if (!nb)
+			L1 = f->p4.L1;
+			L2 = f->p4.L2;
+			if (L1 > FGK_TASK_POINTS || L2 > FGK_TASK_POINTS) {
+				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
-			rb->big = nb;
-			rb->big[rb->nbig].f = f;
-			rb->big[rb->nbig].first = nitems;
-			rb->big[rb->nbig].count = j - i;
-			rb->nbig++;
-			for (; i < j; i++) {
-				items[nitems].in_off = in_offsets[order[i].idx];
-				items[nitems].out_off = out_offsets[order[i].idx];
-				nitems++;
 			}
-			if (2 * (size_t)L > rb->work_floats)
-				rb->work_floats = 2 * (size_t)L;
+			for (k = i; k < j; k++) {
+				fgk_big *b = &bigs[nbig++];
+				b->p4 = f->p4.dev;
+				b->in_off = in_offsets[order[k].idx];
+				b->out_off = out_offsets[order[k].idx];
+				b->scratch_off = scratch_f2;
+				b->ls1 = fsr_lanes_log2(L1, L2);
+				b->ls2 = fsr_lanes_log2(L2, L1);
+				b->ncols = (L2 + (1u << b->ls1) - 1) >> b->ls1;
+				b->nrows = (L1 + (1u << b->ls2) - 1) >> b->ls2;
+				total_cols += b->ncols;
+				cap_tasks += b->ncols + b->nrows;
+				scratch_f2 += ((size_t)L + 15) & ~(size_t)15; /* 128-byte aligned items */
+			}
 		}
-		i = j;
 	}
-	/* work buffer: as many big items at a time as fit the cap (at least one) */
-	if (rb->nbig) {
-		size_t per = rb->work_floats; /* floats per item slot (largest size) */
-		size_t slots = FSR_WORK_CAP / (per * sizeof(float));
-		uint32_t maxc = 0;
-		for (i = 0; i < rb->nbig; i++)
-			if (rb->big[i].count > maxc)
-				maxc = rb->big[i].count;
-		if (slots < 1)
-			slots = 1;
-		if (slots > maxc)
-			slots = maxc;
-		rb->work_floats = per * slots;
-		if ((e = cudaMalloc((void **)&rb->work, rb->work_floats * sizeof(float))) != cudaSuccess)
-			goto cuda_fail;
+	tasks = (fgk_task *)malloc(sizeof(*tasks) * (cap_tasks ? cap_tasks : 1));
+	if (!tasks)
+		goto fail;
+	/* big items: COLS of item b, ROWS of item b - D */
+	if (nbig) {
+		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms);
+		const uint64_t avg = (total_cols + nbig - 1) / nbig;
+		uint32_t D = (uint32_t)((grid + avg - 1) / avg) + 1, b, t;
+		for (b = 0; b < nbig + D; b++) {
+			if (b < nbig)
+				for (t = 0; t < bigs[b].ncols; t++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_COLS, b, t, 0};
+			if (b >= D)
+				for (t = 0; t < bigs[b - D].nrows; t++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_ROWS, b - D, t, 0};
+		}
 	}
-	rb->nchunks = nchunks;
-	if ((e = cudaMalloc((void **)&rb->plans_dev, sizeof(fgk_plan) * (nplans ? nplans : 1))) != cudaSuccess ||
-	    (e = cudaMalloc((void **)&rb->chunks_dev, sizeof(fgk_rg_chunk) * (nchunks ? nchunks : 1))) != cudaSuccess ||
-	    (e = cudaMalloc((void **)&rb->items_dev, sizeof(fgk_rg_item) * n)) != cudaSuccess ||
-	    (e = cudaMalloc((void **)&rb->counter_dev, sizeof(int))) != cudaSuccess)
+	/* small items, largest first */
+	{
+		uint32_t pi = 0;
+		for (i = nbig; i < n; i = j) {
+			const unsigned L = order[i].bins;
+			uint32_t G, tg;
+			for (j = i; j < n && order[j].bins == L; j++)
+				;
+			tg = plans[pi].threads;
+			G = plans[pi].per_cta;
+			for (; i < j;) {
+				const uint32_t m = j - i < G ? j - i : G;
+				uint32_t k;
+				tasks[ntasks++] = (fgk_task){FGK_TASK_SMALL, pi, nitems, m | (tg << 16)};
+				for (k = 0; k < m; k++) {
+					items[nitems].in_off = in_offsets[order[i + k].idx];
+					items[nitems].out_off = out_offsets[order[i + k].idx];
+					nitems++;
+				}
+				i += m;
+			}
+			pi++;
+		}
+	}
+	rb->ntasks = ntasks;
+	rb->nbig = nbig;
+	rb->nbig_items = nbig;
+	if ((e = cudaMalloc((void **)&rb->tasks_dev, sizeof(fgk_task) * (ntasks ? ntasks : 1))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->plans_dev, sizeof(fgk_plan) * (nplans ? nplans : 1))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->items_dev, sizeof(fgk_rg_item) * (nitems ? nitems : 1))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->bigs_dev, sizeof(fgk_big) * (nbig ? nbig : 1))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->counters_dev, sizeof(int) * (1 + (size_t)nbig))) != cudaSuccess ||
+	    (scratch_f2 && (e = cudaMalloc((void **)&rb->scratch, scratch_f2 * 2 * sizeof(float))) != cudaSuccess))
 		goto cuda_fail;
-	if ((nplans && (e = cudaMemcpy(rb->plans_dev, plans, sizeof(fgk_plan) * nplans, cudaMemcpyHostToDevice)) !=
+	if ((e = cudaMemcpy(rb->tasks_dev, tasks, sizeof(fgk_task) * ntasks, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	    (nplans && (e = cudaMemcpy(rb->plans_dev, plans, sizeof(fgk_plan) * nplans, cudaMemcpyHostToDevice)) !=
 	                   cudaSuccess) ||
-	    (nchunks && (e = cudaMemcpy(rb->chunks_dev, chunks, sizeof(fgk_rg_chunk) * nchunks,
-	                                cudaMemcpyHostToDevice)) != cudaSuccess) ||
-	    (e = cudaMemcpy(rb->items_dev, items, sizeof(fgk_rg_item) * n, cudaMemcpyHostToDevice)) != cudaSuccess)
+	    (nitems && (e = cudaMemcpy(rb->items_dev, items, sizeof(fgk_rg_item) * nitems, cudaMemcpyHostToDevice)) !=
+	                   cudaSuccess) ||
+	    (nbig && (e = cudaMemcpy(rb->bigs_dev, bigs, sizeof(fgk_big) * nbig, cudaMemcpyHostToDevice)) != cudaSuccess))
 		goto cuda_fail;
 	if ((e = cudaStreamCreateWithFlags(&rb->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
 		goto cuda_fail;
 	free(order);
 	free(plans);
-	free(chunks);
 	free(items);
+	free(bigs);
+	free(tasks);
 	return rb;
 cuda_fail:
 	cudaGetLastError();
@@ -250,8 +273,9 @@ fail:
 	fs_latch(fs, rc, 0);
 	free(order);
 	free(plans);
-	free(chunks);
 	free(items);
+	free(bigs);
+	free(tasks);
 	fftset_ragged_destroy(rb);
 	return NULL;
 }
@@ -260,25 +284,8 @@ fail:
 static int fsr_record(struct fftset_ragged *rb, float *out, const float *in, cudaStream_t s)
 {
 	struct fs_impl *fs = rb->fs;
-	uint32_t b;
-	int rc = fgk_launch_ragged(rb->plans_dev, rb->chunks_dev, rb->nchunks, rb->items_dev, rb->counter_dev, rb->op, in,
-	                           out, fs->num_sms, s);
-	if (rc)
-		return rc;
-	for (b = 0; b < rb->nbig; b++) {
-		const struct fftset_fft *f = rb->big[b].f;
-		const size_t per = 2 * (size_t)f->lfft;
-		const uint32_t slots = (uint32_t)(rb->work_floats / per);
-		uint32_t done;
-		for (done = 0; done < rb->big[b].count; done += slots) {
-			uint32_t m = rb->big[b].count - done < slots ? rb->big[b].count - done : slots;
-			rc = fgk_launch_fourstep_items(&f->p4, rb->op, out, in, rb->items_dev + rb->big[b].first + done, rb->work,
-			                               m, per, s);
-			if (rc)
-				return rc;
-		}
-	}
-	return 0;
+	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
+	                        rb->counters_dev, rb->scratch, rb->op, in, out, fs->num_sms, fs->dev_flag, s);
 }
 
 int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)
@@ -351,11 +358,5 @@ double fftset_ragged_bytes(const struct fftset_ragged *rb)
 
 unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb)
 {
-	unsigned i, m = 0;
-	if (!rb)
-		return 0;
-	m = rb->n;
-	for (i = 0; i < rb->nbig; i++)
-		m -= rb->big[i].count;
-	return m;
+	return rb ? rb->n : 0; /* every item runs in the one persistent launch */
 }

@@ -76,16 +76,36 @@ typedef struct fgk_plan4 {
 	const struct fgk_plan4 *dev;
 } fgk_plan4;
 
-/* Ragged batches: item offsets (floats, from the batch's base pointers) and
- * chunks of up to n same-size items run side by side in one CTA, tg threads
- * each (fgk_ragged.cu). */
+/* Ragged batches: item offsets in floats from the batch's base pointers. */
 typedef struct fgk_rg_item {
 	uint64_t in_off, out_off;
 } fgk_rg_item;
 
-typedef struct fgk_rg_chunk {
-	uint32_t plan, first, n, tg;
-} fgk_rg_chunk;
+/* Ragged batches as tasks of one persistent launch (fgk_tasks.cu). Every
+ * task is a tile of at most FGK_TASK_POINTS points:
+ *   SMALL  n same-size items (whole transforms, tg threads each);
+ *   COLS   lanes of columns of a big item's four-step split L = L1 L2 (DFTs
+ *          of length L1 from the input, twiddled, into the item's scratch);
+ *   ROWS   lanes of rows of that scratch (DFTs of length L2 into the
+ *          output); they start once every COLS tile of the item is done. */
+#define FGK_TASK_POINTS 4096
+enum fgk_task_kind { FGK_TASK_SMALL = 0, FGK_TASK_COLS = 1, FGK_TASK_ROWS = 2 };
+
+typedef struct fgk_task {
+	uint32_t kind;
+	uint32_t ref;  /* SMALL: plan index; COLS/ROWS: big-item index */
+	uint32_t a;    /* SMALL: first item; COLS/ROWS: tile index */
+	uint32_t b;    /* SMALL: items | threads per item << 16 */
+} fgk_task;
+
+typedef struct fgk_big {
+	const struct fgk_plan4 *p4;            /* device copy of the item's four-step plan */
+	uint64_t                in_off, out_off; /* floats from the batch's base pointers */
+	uint64_t                scratch_off;     /* float2 offset of the item's L1 x L2 scratch */
+	uint32_t                ncols;           /* COLS tiles */
+	uint32_t                ls1, ls2;        /* log2 of the lanes of a COLS / ROWS tile */
+	uint32_t                nrows;           /* ROWS tiles */
+} fgk_big;
 
 /* Host-side planning helpers implemented in fgk_plan.c */
 int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
@@ -110,16 +130,15 @@ uint32_t fgk_max_resident_L(void);
 int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
                         const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
                         size_t out_stride, size_t work_stride, void *stream);
-/* the same for `count` transforms at item offsets (forward / inverse) */
-int fgk_launch_fourstep_items(const fgk_plan4 *p, int op, float *out_base, const float *in_base,
-                              const fgk_rg_item *items_dev, float *work, uint32_t count, size_t work_stride,
-                              void *stream);
-/* one persistent launch over all chunks (fgk_ragged.cu); counter_dev: one
- * int of device scratch, reset by the launcher */
-int    fgk_launch_ragged(const fgk_plan *plans_dev, const fgk_rg_chunk *chunks_dev, uint32_t nchunks,
-                         const fgk_rg_item *items_dev, int *counter_dev, int op, const float *in_base,
-                         float *out_base, int num_sms, void *stream);
-size_t fgk_ragged_smem_bytes(void);
+/* the task launch: counters_dev holds 1 + nbig ints (claim counter, then the
+ * finished COLS tiles of each big item) and is reset by the launcher;
+ * scratch_dev holds the big items' L1 x L2 intermediates; err_flag is set
+ * when a bounded wait gives up */
+int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
+                        const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig, int *counters_dev,
+                        float *scratch_dev, int op, const float *in_base, float *out_base, int num_sms,
+                        int *err_flag, void *stream);
+int    fgk_tasks_grid(int num_sms);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -27,6 +27,7 @@
 #include <stdint.h>
 #include "fgk.h"
 #include "fgk_codelets.cuh"
+#include "fgk_pingpong.cuh"
 
 namespace fgk {
 
@@ -149,8 +150,7 @@ __host__ __device__ __forceinline__ uint32_t lane_groups(uint32_t len, int nl, b
 /* Pass 1: columns. */
 template <int EMAX>
 __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int mode, const float *in, float2 *work,
-                                                          uint32_t count, size_t in_stride, size_t work_stride,
-                                                          const fgk_rg_item *__restrict__ list)
+                                                          uint32_t count, size_t in_stride, size_t work_stride)
 {
 	extern __shared__ float2 smem[];
 	const fgk_plan4 *dp = p.dev;
@@ -171,11 +171,11 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 	const uint32_t grp = blockIdx.x - (uint32_t)(tr * groups);
 	if (tr >= count)
 		return;
-	const float *x = in + (list ? list[tr].in_off : tr * in_stride);
+	const float *x = in + tr * in_stride;
 	float2 *y = work + tr * work_stride;
 
 	const int items = (int)L1 << t.lshift;
-	for (int w = t.tid; w < items; w += t.T) {
+	batched_copy<8>(items, t.tid, t.T, [&](int w) {
 		const int n1 = w >> t.lshift, lane = w & (t.nl - 1);
 		bool valid;
 		const uint32_t n2 = lane_index(grp, lane, t.nl, mirror, L2, valid);
@@ -199,8 +199,7 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 					v = conjf2(__ldcs(X + n));
 			}
 		}
-		t.st(n1, lane, v);
-	}
+		return v; }, [&](int w, float2 v) { t.st(w >> t.lshift, w & (t.nl - 1), v); });
 	__syncthreads();
 	run_chain4<EMAX>(t, &dp->c1, (const float2 *)p.tw1);
 	for (int w = t.tid; w < items; w += t.T) {
@@ -217,7 +216,7 @@ template <int EMAX>
 __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int mode, const float2 *work, float *out,
                                                           uint32_t count, size_t work_stride, size_t out_stride,
                                                           const float *__restrict__ kern, const int32_t *__restrict__ kidx,
-                                                          int kvw, const fgk_rg_item *__restrict__ list)
+                                                          int kvw)
 {
 	extern __shared__ float2 smem[];
 	const fgk_plan4 *dp = p.dev;
@@ -239,16 +238,22 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 	if (tr >= count)
 		return;
 	const float2 *yin = work + tr * work_stride;
-	float *o = out + (list ? list[tr].out_off : tr * out_stride);
+	float *o = out + tr * out_stride;
 	const int half = t.nl >> 1;
 	const int items = (int)L2 << t.lshift;
-	for (int w = t.tid; w < items; w += t.T) {
-		/* consecutive threads read consecutive n2 of one row */
-		const int lane = w / (int)L2, n2 = w - lane * (int)L2;
-		bool valid;
-		const uint32_t k1 = lane_index(grp, lane, t.nl, mirror, L1, valid);
-		t.st(n2, lane, valid ? __ldcs(yin + (uint64_t)k1 * L2 + n2) : make_float2(0.f, 0.f));
-	}
+	/* consecutive threads read consecutive n2 of one row */
+	batched_copy<8>(
+	    items, t.tid, t.T,
+	    [&](int w) {
+		    const int lane = w / (int)L2, n2 = w - lane * (int)L2;
+		    bool valid;
+		    const uint32_t k1 = lane_index(grp, lane, t.nl, mirror, L1, valid);
+		    return valid ? __ldcs(yin + (uint64_t)k1 * L2 + n2) : make_float2(0.f, 0.f);
+	    },
+	    [&](int w, float2 v) {
+		    const int lane = w / (int)L2, n2 = w - lane * (int)L2;
+		    t.st(n2, lane, v);
+	    });
 	__syncthreads();
 	run_chain4<EMAX>(t, &dp->c2, (const float2 *)p.tw2);
 	for (int w = t.tid; w < items; w += t.T) {
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 
 static int launch_pass(const fgk_plan4 *p, int in_mode, int out_mode, float *out, const float *in, float *work,
                        uint32_t count, size_t in_stride, size_t out_stride, size_t work_stride, const float *kern,
-                       const int32_t *kidx, int kvw, cudaStream_t stream, const fgk_rg_item *items = nullptr)
+                       const int32_t *kidx, int kvw, cudaStream_t stream)
 {
 	using namespace fgk;
 	const bool freq = p->modulation == FGK_MOD_FREQOFF;
@@ -324,11 +329,11 @@ static int launch_pass(const fgk_plan4 *p, int in_mode, int out_mode, float *out
 	if (b1 > 0x7fffffffull || b2 > 0x7fffffffull)
 		return (int)cudaErrorInvalidValue;
 	k1<<<(unsigned)b1, p->threads1, sm1, stream>>>(*p, in_mode, in, reinterpret_cast<float2 *>(work), count, in_stride,
-	                                                 work_stride / 2, items);
+	                                                 work_stride / 2);
 	if ((e = cudaGetLastError()) != cudaSuccess)
 		return (int)e;
 	k2<<<(unsigned)b2, p->threads2, sm2, stream>>>(*p, out_mode, reinterpret_cast<const float2 *>(work), out, count,
-	                                                 work_stride / 2, out_stride, kern, kidx, kvw, items);
+	                                                 work_stride / 2, out_stride, kern, kidx, kvw);
 	return (int)cudaGetLastError();
 }
 
@@ -364,20 +369,4 @@ extern "C" int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const
 	default:
 		return (int)cudaErrorInvalidValue;
 	}
-}
-
-extern "C" int fgk_launch_fourstep_items(const fgk_plan4 *p, int op, float *out_base, const float *in_base,
-                                         const fgk_rg_item *items_dev, float *work, uint32_t count,
-                                         size_t work_stride, void *stream)
-{
-	using namespace fgk;
-	if (count == 0)
-		return 0;
-	if (op == FGK_OP_FORWARD)
-		return launch_pass(p, FGK4_IN_FORWARD, FGK4_OUT_FORWARD, out_base, in_base, work, count, 0, 0, work_stride,
-		                   nullptr, nullptr, 0, (cudaStream_t)stream, items_dev);
-	if (op == FGK_OP_INVERSE)
-		return launch_pass(p, FGK4_IN_INVERSE, FGK4_OUT_FINAL, out_base, in_base, work, count, 0, 0, work_stride,
-		                   nullptr, nullptr, 0, (cudaStream_t)stream, items_dev);
-	return (int)cudaErrorInvalidValue;
 }

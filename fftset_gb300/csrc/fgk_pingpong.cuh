@@ -61,6 +61,29 @@ __device__ __forceinline__ void rg_stage(const float2 *src, float2 *dst, int L, 
 	}
 }
 
+/* n elements from ld(i) to st(i, v), this thread's i = tid, tid + T, ...,
+ * U loads in flight per thread: HBM needs tens of KB in flight per SM, which
+ * one dependent load per loop iteration does not provide. */
+template <int U, class Ld, class St>
+__device__ __forceinline__ void batched_copy(int n, int tid, int T, Ld &&ld, St &&st)
+{
+	for (int base = tid; base < n; base += U * T) {
+		float2 v[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			const int i = base + u * T;
+			if (i < n)
+				v[u] = ld(i);
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			const int i = base + u * T;
+			if (i < n)
+				st(i, v[u]);
+		}
+	}
+}
+
 /* The plan's forward chain over buffers a/b, starting from a (which holds
  * the natural-order input). Returns the buffer that holds the natural-order
  * DFT. `sync` is the group's barrier, called after every stage. */

@@ -162,10 +162,12 @@ int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, fl
  * same modulation, op FFTSET_OP_FORWARD or FFTSET_OP_INVERSE), item i read
  * from input_base + in_offsets[i] and written to output_base + out_offsets[i]
  * (offsets in floats, even; device buffers). All sizes share the fftset's
- * plans and twiddles. Sizes whose two shared-memory buffers fit one CTA run
- * in one persistent launch; larger ones run the four-step passes; the
- * sequence is captured in a CUDA graph on the first execute (again when the
- * base pointers change) and replayed. */
+ * plans and twiddles. Every item runs in one persistent launch of tile tasks
+ * (items up to 4096 bins whole; larger ones as the column and row tiles of
+ * their four-step split, through a scratch buffer that L2 serves), captured
+ * in a CUDA graph on the first execute (again when the base pointers change)
+ * and replayed. fftset_ragged_execute reports FFTSET_E_TIMEOUT if a tile's
+ * bounded wait gave up. */
 struct fftset_ragged;
 struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftset_modulation *modulation, int op,
                                            unsigned n, const unsigned *bins, const size_t *in_offsets,
