@@ -162,7 +162,7 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 	fgk_plan4 *p = &f->p4;
 	const unsigned L = f->lfft;
 	const uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
-	size_t n1, n2, nhi, off[10], total, i;
+	size_t n1, n2, nhi, nlo, off[10], total, i;
 	float *h = NULL;
 	char *d = NULL;
 	int32_t *kidx = NULL;
@@ -176,10 +176,16 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		return FFTSET_E_UNSUPPORTED;
 	n1 = fgk_chain_twiddles(&p->c1, NULL);
 	n2 = fgk_chain_twiddles(&p->c2, NULL);
-	nhi = (L + 4095) / 4096;
+	/* w_L^m = thi[m >> tshift] tlo[m & (2^tshift - 1)], both tables about
+	 * sqrt(L) entries so that they stay in L1 */
+	p->tshift = 1;
+	while (((uint64_t)1 << (2 * p->tshift)) < L)
+		p->tshift++;
+	nlo = (size_t)1 << p->tshift;
+	nhi = (L + nlo - 1) / nlo;
 	/* float2 counts: tw1, tw2, thi, tlo, m1, m2, n1, n2; then kidx (int32) and the plan copy */
 	{
-		const size_t cnt[8] = {n1 ? n1 : 1, n2 ? n2 : 1, nhi, 4096, p->L1, p->L2, p->L1, p->L2};
+		const size_t cnt[8] = {n1 ? n1 : 1, n2 ? n2 : 1, nhi, nlo, p->L1, p->L2, p->L1, p->L2};
 		total = fs_align(sizeof(fgk_plan4));
 		for (i = 0; i < 8; i++) {
 			off[i] = total;
@@ -188,7 +194,7 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		off[8] = total;
 		total += fs_align(sizeof(int32_t) * L);
 	}
-	h = (float *)malloc(sizeof(float) * 2 * (n1 + n2 + nhi + 4096 + 2 * (size_t)p->L1 + 2 * (size_t)p->L2 + 2));
+	h = (float *)malloc(sizeof(float) * 2 * (n1 + n2 + nhi + nlo + 2 * (size_t)p->L1 + 2 * (size_t)p->L2 + 2));
 	kidx = (int32_t *)malloc(sizeof(int32_t) * L);
 	if (!h || !kidx)
 		goto out;
@@ -210,16 +216,16 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		fgk_chain_twiddles(&p->c2, tw2);
 		thi = tw2 + 2 * (n2 ? n2 : 1);
 		tlo = thi + 2 * nhi;
-		m1 = tlo + 2 * 4096;
+		m1 = tlo + 2 * nlo;
 		m2 = m1 + 2 * (size_t)p->L1;
 		q1 = m2 + 2 * (size_t)p->L2;
 		q2 = q1 + 2 * (size_t)p->L1;
 		for (k = 0; k < nhi; k++) {
-			double a = -2.0 * M_PI * (double)(k * 4096) / (double)L;
+			double a = -2.0 * M_PI * (double)(k * nlo) / (double)L;
 			thi[2 * k] = (float)cos(a);
 			thi[2 * k + 1] = (float)sin(a);
 		}
-		for (k = 0; k < 4096; k++) {
+		for (k = 0; k < nlo; k++) {
 			double a = -2.0 * M_PI * (double)k / (double)L;
 			tlo[2 * k] = (float)cos(a);
 			tlo[2 * k + 1] = (float)sin(a);
@@ -240,7 +246,7 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		}
 		{
 			float *srcs[8] = {tw1, tw2, thi, tlo, m1, m2, q1, q2};
-			const size_t cnt[8] = {n1, n2, nhi, 4096, p->L1, p->L2, p->L1, p->L2};
+			const size_t cnt[8] = {n1, n2, nhi, nlo, p->L1, p->L2, p->L1, p->L2};
 			const void **dst[8] = {&p->tw1, &p->tw2, &p->thi, &p->tlo, &p->m1, &p->m2, &p->n1, &p->n2};
 			for (k = 0; k < 8; k++) {
 				*dst[k] = d + off[k];

@@ -23,7 +23,7 @@
 #include "fftset_internal.h"
 #include "fgk.h"
 
-#define FSR_THREADS 256 /* threads of a task CTA */
+#define FSR_THREADS ((uint32_t)fgk_tasks_threads()) /* threads of a task CTA */
 
 struct fftset_ragged {
 	struct fs_impl *fs;
@@ -196,7 +196,8 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 				b->nrows = (L1 + (1u << b->ls2) - 1) >> b->ls2;
 				total_cols += b->ncols;
 				cap_tasks += b->ncols + b->nrows;
-				scratch_f2 += ((size_t)L + 15) & ~(size_t)15; /* 128-byte aligned items */
+				/* laid out by ROWS tiles (full tiles), 128-byte aligned items */
+				scratch_f2 += ((((size_t)b->nrows * L2) << b->ls2) + 15) & ~(size_t)15;
 			}
 		}
 	}

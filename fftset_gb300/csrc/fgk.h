@@ -70,7 +70,8 @@ typedef struct fgk_plan4 {
 	uint32_t  emax1, emax2;
 	fgk_chain c1, c2;
 	const void *tw1, *tw2;      /* chain twiddles */
-	const void *thi, *tlo;      /* w_L^m = thi[m >> 12] * tlo[m & 4095] */
+	uint32_t  tshift;           /* w_L^m = thi[m >> tshift] * tlo[m & ((1 << tshift) - 1)] */
+	const void *thi, *tlo;
 	const void *m1, *m2;        /* e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2L)}: input modulation */
 	const void *n1, *n2;        /* e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2)}: output modulation */
 	const struct fgk_plan4 *dev;
@@ -139,6 +140,7 @@ int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_pl
                         float *scratch_dev, int op, const float *in_base, float *out_base, int num_sms,
                         int *err_flag, void *stream);
 int    fgk_tasks_grid(int num_sms);
+int    fgk_tasks_threads(void);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -21,8 +21,8 @@
  *   inverse (both): pass 1 loads conj(W), FREQ_OFFSET_REAL mirror columns
  *     L2-1-n2 in the upper lanes; pass 2 applies the final step
  *     (src/fftset_mod_freqoffsetreal.c:974-1010, src/fftset_mod_cplx.c:212-239).
- * The twiddle w_L^{m}, m = n2 k1 < L, is T_hi[m >> 12] * T_lo[m & 4095]:
- * two FP64-generated tables rounded once to FP32. */
+ * The twiddle w_L^{m}, m = n2 k1 < L, is T_hi[m >> s] * T_lo[m & (2^s - 1)]
+ * with 2^s about sqrt(L): two FP64-generated tables rounded once to FP32. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "fgk.h"
@@ -116,8 +116,8 @@ __device__ __forceinline__ void run_chain4(const Tile4 &t, const fgk_chain *ch, 
 
 __device__ __forceinline__ float2 wl(const fgk_plan4 &p, uint64_t m)
 {
-	const float2 hi = __ldg((const float2 *)p.thi + (m >> 12));
-	const float2 lo = __ldg((const float2 *)p.tlo + (m & 4095));
+	const float2 hi = __ldg((const float2 *)p.thi + (m >> p.tshift));
+	const float2 lo = __ldg((const float2 *)p.tlo + (m & ((1u << p.tshift) - 1)));
 	return cmul(hi, lo);
 }
 

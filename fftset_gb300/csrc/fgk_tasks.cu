@@ -11,11 +11,14 @@
  *          by side (tg threads each), HBM in, HBM out.
  *   COLS   a big item (L > FGK_TASK_POINTS) split L = L1 L2 (the fftset's
  *          four-step plan: n = L2 n1 + n2, k = k1 + L1 k2): 2^ls1 adjacent
- *          columns n2, each a DFT of length L1 over n1 read straight from
- *          the input (row segments of 2^ls1 elements), multiplied by
- *          w_L^{n2 k1} and written row-major into the item's scratch.
- *   ROWS   2^ls2 adjacent rows k1 of that scratch, DFTs of length L2 over
- *          n2, written to X[k1 + L1 k2] (segments of 2^ls2 elements).
+ *          columns n2, each a DFT of length L1 over n1 whose first stage
+ *          reads the input directly (row segments of 2^ls1 elements) and
+ *          whose last stage multiplies by w_L^{n2 k1} and writes the item's
+ *          scratch directly, in the order the ROWS tiles read it.
+ *   ROWS   2^ls2 adjacent rows k1 of that scratch (one contiguous block),
+ *          DFTs of length L2 over n2, the last stage writing X[k1 + L1 k2]
+ *          directly (segments of 2^ls2 elements).
+ * Only the middle stages of a big-item tile go through shared memory.
  *
  * A ROWS task waits for all COLS tasks of its item: each COLS task bumps the
  * item's counter after its stores are visible (threadfence), and a ROWS task
@@ -38,7 +41,13 @@
 
 namespace fgk {
 
-constexpr int TK_THREADS = 256;
+#ifndef FGKT_THREADS
+#define FGKT_THREADS 256 /* threads of a task CTA */
+#endif
+#ifndef FGKT_MIN_CTAS
+#define FGKT_MIN_CTAS 3 /* resident CTAs per SM the registers are budgeted for */
+#endif
+constexpr int TK_THREADS = FGKT_THREADS;
 constexpr int TK_SLOTS = FGK_TASK_POINTS + FGK_TASK_POINTS / 16 + 1; /* rslots(FGK_TASK_POINTS) */
 constexpr uint32_t TK_SPIN_LIMIT = 1u << 22;                         /* x 256 ns: about a second */
 
@@ -85,30 +94,127 @@ __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int L
 	}
 }
 
-/* chain `ch` over the tile in a/b (input in a); returns the result buffer */
-__device__ __forceinline__ float2 *lane_chain(const fgk_chain *ch, const float2 *tw, int Lp, int ls, float2 *a,
-                                              float2 *b, int tid, int T)
+/* ---- tiles: first and last stages straight from and to memory ---------- */
+/* First stage of a tile (ns = 1, no twiddles) straight from memory:
+ * butterfly j of lane l reads ld(j + p nbf, l) (lanes fastest, so a warp
+ * reads consecutive lanes of one element: the row segments in memory). */
+template <int R, class Ld>
+__device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls, int tid, int T)
+{
+	const int nbf = Lp / R;
+	const int items = nbf << ls;
+	const int lm = (1 << ls) - 1;
+	for (int w = tid; w < items; w += T) {
+		const int j = w >> ls, lane = w & lm;
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = ld(j + p * nbf, lane);
+		Radix<R>::run(v);
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			dst[rslot(((j * R + q) << ls) + lane)] = v[q];
+	}
+}
+
+/* Last stage of a tile (ns = Lp/R: butterfly j twiddled by w^{p j},
+ * outputs j + q nbf) straight to memory through st(k, lane, v). JF: a warp
+ * takes consecutive butterflies j of one lane (consecutive outputs k),
+ * otherwise consecutive lanes of one butterfly. */
+template <int R, bool JF, class St>
+__device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, int ls, const float2 *__restrict__ tw,
+                                          int tid, int T)
+{
+	const int nbf = Lp / R;
+	const int items = nbf << ls;
+	const int lm = (1 << ls) - 1;
+	const float inv = 1.0f / (float)nbf;
+	for (int w = tid; w < items; w += T) {
+		int j, lane;
+		if (JF) {
+			lane = tk_div(w, nbf, inv);
+			j = w - lane * nbf;
+		} else {
+			j = w >> ls;
+			lane = w & lm;
+		}
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = src[rslot(((j + p * nbf) << ls) + lane)];
+		if (nbf > 1) {
+			const float2 *t = tw + j * (R - 1);
+#pragma unroll
+			for (int p = 1; p < R; p++)
+				v[p] = cmul(v[p], __ldg(t + p - 1));
+		}
+		Radix<R>::run(v);
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			st(j + q * nbf, lane, v[q]);
+	}
+}
+
+/* A single-stage chain (Lp = R): memory to memory */
+template <int R, class Ld, class St>
+__device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, int T)
+{
+	const int lanes = 1 << ls;
+	for (int lane = tid; lane < lanes; lane += T) {
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = ld(p, lane);
+		Radix<R>::run(v);
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			st(q, lane, v[q]);
+	}
+}
+
+/* The whole chain of a tile: first stage from ld, middle stages in shared
+ * memory (A/B ping-pong), last stage to st. `after_first` runs once the first
+ * stage is done (all of its reads have returned). Threads with active ==
+ * false only take part in the barriers. */
+template <bool JF, class Ld, class St, class After>
+__device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw, int Lp, int ls, float2 *A,
+                                           float2 *B, int tid, int T, bool active, Ld &&ld, St &&st,
+                                           After &&after_first)
 {
 	const int n = (int)ch->nstages;
-	float2 *src = a, *dst = b;
-	for (int s = 0; s < n; s++) {
-		const fgk_stage st = ch->st[s];
-		FGKR_RADIX_SWITCH(st.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)st.ns, tw + st.tw_off, tid, T)));
+	if (n == 1) {
+		if (active)
+			FGKR_RADIX_SWITCH(ch->st[0].radix, (lane_single<R_>(ld, st, ls, tid, T)));
+		__syncthreads();
+		after_first();
+		return;
+	}
+	if (active) {
+		const fgk_stage st0 = ch->st[0];
+		FGKR_RADIX_SWITCH(st0.radix, (lane_first<R_>(ld, A, Lp, ls, tid, T)));
+	}
+	__syncthreads();
+	after_first();
+	float2 *src = A, *dst = B;
+	for (int s = 1; s < n - 1; s++) {
+		const fgk_stage sm = ch->st[s];
+		if (active)
+			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tw + sm.tw_off, tid, T)));
 		__syncthreads();
 		float2 *t = src;
 		src = dst;
 		dst = t;
 	}
-	return src;
-}
-
-/* w_L^m = thi[m >> 12] tlo[m & 4095] */
-__device__ __forceinline__ float2 tk_wl(const fgk_plan4 *p, uint64_t m)
-{
-	return cmul(__ldg((const float2 *)p->thi + (m >> 12)), __ldg((const float2 *)p->tlo + (m & 4095)));
+	if (active) {
+		const fgk_stage sl = ch->st[n - 1];
+		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tw + sl.tw_off, tid, T)));
+	}
 }
 
 /* ---- SMALL: whole items side by side ---------------------------------- */
+/* n items of one size, tg threads each (group g = threadIdx / tg), each
+ * group's first stage reading its item and its last stage writing its
+ * output directly. */
 __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *__restrict__ plans,
                                            const fgk_rg_item *__restrict__ items, int op, const float *in_base,
                                            float *out_base, float2 *smem)
@@ -116,139 +222,114 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 	const fgk_plan *pl = plans + tk.ref;
 	const int L = (int)pl->L;
 	const bool freq = pl->modulation == FGK_MOD_FREQOFF;
-	const float2 *mod = (const float2 *)pl->modtw;
+	const bool inverse = op == FGK_OP_INVERSE;
 	const int n = (int)(tk.b & 0xffff), T = (int)(tk.b >> 16);
 	const int g = (int)threadIdx.x / T;
 	const int tid = (int)threadIdx.x - g * T;
 	const bool active = g < n;
-	const int slots = rslots(L);
-	float2 *buf0 = smem + (size_t)(active ? g : 0) * 2 * slots;
-	float2 *buf1 = buf0 + slots;
+	float2 *buf0 = smem + (size_t)(active ? g : 0) * 2 * rslots(L);
 	const fgk_rg_item it = active ? items[tk.a + g] : fgk_rg_item{0, 0};
 	const float *x = in_base + it.in_off;
+	const float2 *X = reinterpret_cast<const float2 *>(x);
 	float *y = out_base + it.out_off;
-
-	if (active) {
-		if (op != FGK_OP_INVERSE) {
-			if (freq) {
-				batched_copy<8>(
-				    L, tid, T, [&](int i) { return make_float2(__ldcs(x + i), -__ldcs(x + L + i)); },
-				    [&](int i, float2 v) { buf0[rslot(i)] = cmul(v, __ldg(mod + i)); });
-			} else {
-				const float2 *x2 = reinterpret_cast<const float2 *>(x);
-				batched_copy<8>(
-				    L, tid, T, [&](int i) { return __ldcs(x2 + i); }, [&](int i, float2 v) { buf0[rslot(i)] = v; });
-			}
-		} else {
-			const float2 *X = reinterpret_cast<const float2 *>(x);
-			if (freq) {
-				/* conj W[i]: W[i] = X[2i] for i < ceil(L/2), conj X[2(L-1-i)+1] after */
-				const int hc = (L + 1) >> 1;
-				batched_copy<8>(
-				    L, tid, T,
-				    [&](int i) { return i < hc ? conjf2(__ldcs(X + 2 * i)) : __ldcs(X + 2 * (L - 1 - i) + 1); },
-				    [&](int i, float2 v) { buf0[rslot(i)] = v; });
-			} else {
-				batched_copy<8>(
-				    L, tid, T, [&](int i) { return __ldcs(X + i); },
-				    [&](int i, float2 v) { buf0[rslot(i)] = conjf2(v); });
-			}
+	float2 *y2 = reinterpret_cast<float2 *>(y);
+	const float2 *mod = (const float2 *)pl->modtw;
+	const int hc = (L + 1) >> 1;
+	auto ld = [&](int i, int) {
+		if (!inverse) {
+			if (freq)
+				return cmul(make_float2(__ldcs(x + i), -__ldcs(x + L + i)), __ldg(mod + i));
+			return __ldcs(X + i);
 		}
-	}
-	__syncthreads();
-	const float2 *src = rg_chain(pl, buf0, buf1, active, tid, T, [] { __syncthreads(); });
-	if (active) {
-		float2 *y2 = reinterpret_cast<float2 *>(y);
-		if (op == FGK_OP_INVERSE) {
-			if (freq) {
-				for (int i = tid; i < L; i += T) {
-					const float2 r = cmul(src[rslot(i)], __ldg(mod + i));
-					__stcs(y + i, r.x);
-					__stcs(y + L + i, r.y);
-				}
-			} else {
-				for (int i = tid; i < L; i += T)
-					__stcs(y2 + i, conjf2(src[rslot(i)]));
-			}
+		/* conj W[i]: W[i] = X[2i] for i < ceil(L/2), conj X[2(L-1-i)+1] after */
+		if (freq)
+			return i < hc ? conjf2(__ldcs(X + 2 * i)) : __ldcs(X + 2 * (L - 1 - i) + 1);
+		return conjf2(__ldcs(X + i));
+	};
+	auto st = [&](int k, int, float2 v) {
+		if (!inverse) {
+			if (!freq)
+				__stcs(y2 + k, v);
+			else if (k < hc)
+				__stcs(y2 + 2 * k, v);
+			else
+				__stcs(y2 + 2 * (L - 1 - k) + 1, conjf2(v));
 		} else if (freq) {
-			const int hc = (L + 1) >> 1;
-			for (int i = tid; i < L; i += T) {
-				const float2 v = src[rslot(i)];
-				if (i < hc)
-					__stcs(y2 + 2 * i, v);
-				else
-					__stcs(y2 + 2 * (L - 1 - i) + 1, conjf2(v));
-			}
+			const float2 r = cmul(v, __ldg(mod + k));
+			__stcs(y + k, r.x);
+			__stcs(y + L + k, r.y);
 		} else {
-			for (int i = tid; i < L; i += T)
-				__stcs(y2 + i, src[rslot(i)]);
+			__stcs(y2 + k, conjf2(v));
 		}
-	}
+	};
+	tile_chain<false>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st, [] {});
 }
 
-/* ---- COLS: columns of a big item into its scratch ---------------------- */
+/* COLS: columns n2base .. n2base + 2^ls1 - 1, DFTs of length L1 from the
+ * input into the item's scratch, which is laid out by ROWS tiles: element
+ * (k1, n2) at ((k1 >> ls2) L2 + n2) 2^ls2 + (k1 & (2^ls2 - 1)), so a ROWS
+ * tile reads one contiguous block with its lanes fastest. */
 __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, int op, const float *in_base,
                                           float2 *scratch, int *done, float2 *smem)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
 	const uint64_t L = (uint64_t)L1 * L2;
-	const int ls = (int)bg.ls1, lm = (1 << ls) - 1;
+	const int ls = (int)bg.ls1;
+	const int ls2 = (int)bg.ls2, lm2 = (1 << ls2) - 1;
 	const int n2base = (int)(tk.a << ls);
 	const bool freq = p->modulation == FGK_MOD_FREQOFF;
 	const bool inverse = op == FGK_OP_INVERSE;
 	const float *x = in_base + bg.in_off;
 	const float2 *x2 = reinterpret_cast<const float2 *>(x);
 	const float2 *m1 = (const float2 *)p->m1, *m2 = (const float2 *)p->m2;
-	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
-	float2 *A = smem, *B = smem + TK_SLOTS;
-
-	batched_copy<8>(
-	    L1 << ls, tid, T,
-	    [&](int w) {
-		    const int n1 = w >> ls, n2 = n2base + (w & lm);
-		    if (n2 >= L2)
-			    return make_float2(0.f, 0.f);
-		    const uint64_t n = (uint64_t)n1 * L2 + n2;
-		    if (!inverse) {
-			    if (freq)
-				    return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), cmul(__ldg(m1 + n1), __ldg(m2 + n2)));
-			    return __ldcs(x2 + n);
-		    }
-		    if (freq)
-			    return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
-		    return conjf2(__ldcs(x2 + n));
-	    },
-	    [&](int w, float2 v) { A[rslot(w)] = v; });
-	__syncthreads();
-	const float2 *R = lane_chain(&p->c1, (const float2 *)p->tw1, L1, ls, A, B, tid, T);
+	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo;
+	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
 	float2 *S = scratch + bg.scratch_off;
-	for (int w = tid; w < (L1 << ls); w += T) {
-		const int k1 = w >> ls, n2 = n2base + (w & lm);
-		if (n2 < L2)
-			__stcg(S + (uint64_t)k1 * L2 + n2, cmul(R[rslot(w)], tk_wl(p, (uint64_t)n2 * (uint32_t)k1)));
-	}
+	auto ld = [&](int n1, int lane) {
+		const int n2 = n2base + lane;
+		if (n2 >= L2)
+			return make_float2(0.f, 0.f);
+		const uint64_t n = (uint64_t)n1 * L2 + n2;
+		if (!inverse) {
+			if (freq)
+				return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), cmul(__ldg(m1 + n1), __ldg(m2 + n2)));
+			return __ldcs(x2 + n);
+		}
+		if (freq)
+			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
+		return conjf2(__ldcs(x2 + n));
+	};
+	auto st = [&](int k1, int lane, float2 v) {
+		const int n2 = n2base + lane;
+		if (n2 >= L2)
+			return;
+		const uint32_t m = (uint32_t)n2 * (uint32_t)k1;
+		const float2 w = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		__stcg(S + (((uint64_t)(k1 >> ls2) * L2 + n2) << ls2) + (k1 & lm2), cmul(v, w));
+	};
+	tile_chain<true>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                 (int)blockDim.x, true, ld, st, [] {});
 	__threadfence();
 	__syncthreads();
-	if (tid == 0)
+	if (threadIdx.x == 0)
 		atomicAdd(done, 1);
 }
 
-/* ---- ROWS: rows of the scratch into the output -------------------------- */
+/* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
+ * into X[k1 + L1 k2] */
 __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, int op, float *out_base,
-                                          float2 *scratch, const int *done, int *err, float2 *smem)
+                                          float2 *scratch, const int *done, int *err, float2 *smem, int *failed)
 {
-	__shared__ int failed;
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
 	const uint64_t L = (uint64_t)L1 * L2;
-	const int ls = (int)bg.ls2, nl = 1 << ls, lm = nl - 1;
+	const int ls = (int)bg.ls2, nl = 1 << ls;
 	const int k1base = (int)(tk.a << ls);
+	const int nrow = min(nl, L1 - k1base);
 	const bool freq = p->modulation == FGK_MOD_FREQOFF;
 	const bool inverse = op == FGK_OP_INVERSE;
 	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
-	float2 *A = smem, *B = smem + TK_SLOTS;
-	float2 *S = scratch + bg.scratch_off;
 
 	/* every COLS tile of this item, bounded */
 	if (tid == 0) {
@@ -268,44 +349,22 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 			__nanosleep(256);
 		}
 		__threadfence();
-		failed = f;
+		*failed = f;
 	}
 	__syncthreads();
-	if (failed)
-		return; /* the caller's barrier ends the task */
+	if (*failed)
+		return;
 
-	const int nrow = min(nl, L1 - k1base); /* rows of this tile */
-	const float inv = 1.0f / (float)L2;
-	const float2 *Srow = S + (uint64_t)k1base * L2;
-	batched_copy<8>(
-	    nrow * L2, tid, T, [&](int w) { return __ldcg(Srow + w); },
-	    [&](int w, float2 v) {
-		    const int lane = tk_div(w, L2, inv), n2 = w - lane * L2;
-		    A[rslot((n2 << ls) + lane)] = v;
-	    });
-	if (nrow < nl) /* lanes past the last row hold zeros */
-		for (int w = tid; w < (L2 << ls); w += T)
-			if ((w & lm) >= nrow)
-				A[rslot(w)] = make_float2(0.f, 0.f);
-	__syncthreads();
-	/* the rows are consumed: drop their L2 lines without writing them back */
-	{
-		const uintptr_t b0 = (reinterpret_cast<uintptr_t>(Srow) + 127) & ~(uintptr_t)127;
-		const uintptr_t b1 = reinterpret_cast<uintptr_t>(Srow + (uint64_t)nrow * L2) & ~(uintptr_t)127;
-		for (uintptr_t a = b0 + (uintptr_t)tid * 128; a < b1; a += (uintptr_t)T * 128)
-			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
-	}
-	const float2 *R = lane_chain(&p->c2, (const float2 *)p->tw2, L2, ls, A, B, tid, T);
+	const float2 *Stile = scratch + bg.scratch_off + (uint64_t)tk.a * ((uint64_t)L2 << ls);
 	float *o = out_base + bg.out_off;
 	float2 *o2 = reinterpret_cast<float2 *>(o);
 	const float2 *q1 = (const float2 *)p->n1, *q2 = (const float2 *)p->n2;
-	for (int w = tid; w < (L2 << ls); w += T) {
-		const int k2 = w >> ls, lane = w & lm;
+	auto ld = [&](int n2, int lane) { return __ldcg(Stile + ((uint64_t)n2 << ls) + lane); };
+	auto st = [&](int k2, int lane, float2 v) {
 		if (lane >= nrow)
-			continue;
+			return;
 		const int k1 = k1base + lane;
 		const uint64_t m = (uint64_t)k1 + (uint64_t)L1 * k2;
-		const float2 v = R[rslot(w)];
 		if (!inverse) {
 			if (!freq)
 				__stcs(o2 + m, v);
@@ -320,39 +379,69 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		} else {
 			__stcs(o2 + m, conjf2(v));
 		}
-	}
+	};
+	/* once the first stage has read the tile, drop its L2 lines without
+	 * writing them back */
+	auto discard = [&] {
+		const uintptr_t b0 = reinterpret_cast<uintptr_t>(Stile);
+		const uintptr_t b1 = b0 + ((uintptr_t)L2 << ls) * sizeof(float2);
+		for (uintptr_t a = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)tid * 128; a + 128 <= b1; a += (uintptr_t)T * 128)
+			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+	};
+	tile_chain<false>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st, discard);
 }
 
-__global__ void __launch_bounds__(TK_THREADS, 3)
+/* One CTA: run tasks in claim order. Thread 0 claims the next task as the
+ * current one starts, so the claim's round trip overlaps the work. */
+__global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs, int *counters,
                 float2 *scratch, int op, const float *in_base, float *out_base, int *err)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
+	__shared__ fgk_task next_task;
+	__shared__ int failed;
+	uint32_t ahead = 0;
+	if (threadIdx.x == 0) {
+		cur = (uint32_t)atomicAdd(counters, 1);
+		if (cur < ntasks)
+			next_task = tasks[cur];
+	}
+	__syncthreads();
 	for (;;) {
-		if (threadIdx.x == 0)
-			cur = (uint32_t)atomicAdd(counters, 1);
-		__syncthreads();
 		const uint32_t c = cur;
 		if (c >= ntasks)
 			break;
-		const fgk_task tk = tasks[c];
+		const fgk_task tk = next_task;
+		if (threadIdx.x == 0)
+			ahead = (uint32_t)atomicAdd(counters, 1);
 		if (tk.kind == FGK_TASK_SMALL)
 			task_small(tk, plans, items, op, in_base, out_base, smem);
 		else if (tk.kind == FGK_TASK_COLS)
 			task_cols(tk, bigs[tk.ref], op, in_base, scratch, counters + 1 + tk.ref, smem);
 		else
-			task_rows(tk, bigs[tk.ref], op, out_base, scratch, counters + 1 + tk.ref, err, smem);
-		__syncthreads(); /* buffers and `cur` are reused by the next task */
+			task_rows(tk, bigs[tk.ref], op, out_base, scratch, counters + 1 + tk.ref, err, smem, &failed);
+		__syncthreads(); /* buffers are reused by the next task */
+		if (threadIdx.x == 0) {
+			cur = ahead;
+			if (ahead < ntasks)
+				next_task = tasks[ahead];
+		}
+		__syncthreads();
 	}
 }
 
 } /* namespace fgk */
 
+extern "C" int fgk_tasks_threads(void)
+{
+	return FGKT_THREADS;
+}
+
 extern "C" int fgk_tasks_grid(int num_sms)
 {
-	return 3 * num_sms;
+	return FGKT_MIN_CTAS * num_sms;
 }
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
