@@ -3,8 +3,8 @@
  * fftset_ragged_create plans every distinct size through the fftset's own
  * plan cache (fftset_create_fft, so all sizes share the fftset's twiddle
  * tables) and builds the task list of one persistent launch
- * (fgk_tasks.cu), every task a tile of at most FGK_TASK_POINTS points:
- *   - items up to FGK_TASK_POINTS bins: SMALL tasks of same-size items;
+ * (fgk_tasks.cu), every task a tile of at most fgk_tasks_points() points:
+ *   - items up to fgk_tasks_points() bins: SMALL tasks of same-size items;
  *   - larger items: their four-step split L = L1 L2, COLS tiles (columns
  *     into the item's scratch) then ROWS tiles (rows into the output). The
  *     ROWS tiles of item i are listed after the COLS tiles of item i + D,
@@ -28,6 +28,7 @@
 struct fftset_ragged {
 	struct fs_impl *fs;
 	int             op;
+	int             modulation; /* FGK_MOD_* */
 	unsigned        n;
 	fgk_task       *tasks_dev;
 	uint32_t        ntasks;
@@ -65,14 +66,15 @@ static uint32_t fsr_slots(uint32_t L)
 	return L + L / 16 + 1;
 }
 
-/* threads per item of a SMALL task: enough for the widest stage, a multiple
- * of 32, at most the CTA */
+/* threads per item of a SMALL task: the butterflies of the narrowest stage
+ * (so that every stage keeps all threads busy; wider stages loop), a
+ * multiple of 32, at most the CTA */
 static uint32_t fsr_item_threads(const fgk_plan *p)
 {
-	uint32_t s, w = 1;
+	uint32_t s, w = p->L;
 	for (s = 0; s < p->fwd.nstages; s++) {
 		uint32_t nbf = p->L / p->fwd.st[s].radix;
-		if (nbf > w)
+		if (nbf < w)
 			w = nbf;
 	}
 	w = (w + 31) & ~31u;
@@ -80,11 +82,11 @@ static uint32_t fsr_item_threads(const fgk_plan *p)
 }
 
 /* log2 of the lanes of a tile of columns (rows) of length lp: as many as
- * FGK_TASK_POINTS holds, no more than the `count` columns (rows) there are */
+ * a tile holds, no more than the `count` columns (rows) there are */
 static uint32_t fsr_lanes_log2(uint32_t lp, uint32_t count)
 {
 	uint32_t ls = 0;
-	while ((lp << (ls + 1)) <= FGK_TASK_POINTS && (1u << ls) < count)
+	while ((lp << (ls + 1)) <= (uint32_t)fgk_tasks_points() && (1u << ls) < count)
 		ls++;
 	return ls;
 }
@@ -145,6 +147,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 		goto fail;
 	rb->fs = fs;
 	rb->op = op;
+	rb->modulation = modulation->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
 	rb->n = n;
 	rb->use_graph = 1;
 	for (i = 0; i < n; i++) {
@@ -164,11 +167,11 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 			rc = FFTSET_E_INVALID;
 			goto fail;
 		}
-		if (!f->fourstep && L <= FGK_TASK_POINTS) {
+		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
 			const uint32_t tg = fsr_item_threads(&f->rp);
 			uint32_t G = FSR_THREADS / tg;
-			if (G * fsr_slots(L) > fsr_slots(FGK_TASK_POINTS))
-				G = fsr_slots(FGK_TASK_POINTS) / fsr_slots(L);
+			if (G * fsr_slots(L) > (uint32_t)fgk_tasks_slots())
+				G = (uint32_t)fgk_tasks_slots() / fsr_slots(L);
 			plans[nplans] = f->rp;
 			cap_tasks += (j - i + G - 1) / G;
 			plans[nplans].threads = tg; /* reused below: threads per item */
@@ -180,7 +183,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 				goto fail;
 			L1 = f->p4.L1;
 			L2 = f->p4.L2;
-			if (L1 > FGK_TASK_POINTS || L2 > FGK_TASK_POINTS) {
+			if (L1 > (uint32_t)fgk_tasks_points() || L2 > (uint32_t)fgk_tasks_points()) {
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
 			}
@@ -286,7 +289,8 @@ static int fsr_record(struct fftset_ragged *rb, float *out, const float *in, cud
 {
 	struct fs_impl *fs = rb->fs;
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
-	                        rb->counters_dev, rb->scratch, rb->op, in, out, fs->num_sms, fs->dev_flag, s);
+	                        rb->counters_dev, rb->scratch, rb->op, rb->modulation, in, out, fs->num_sms, fs->dev_flag,
+	                        s);
 }
 
 int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)

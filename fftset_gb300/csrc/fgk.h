@@ -83,13 +83,13 @@ typedef struct fgk_rg_item {
 } fgk_rg_item;
 
 /* Ragged batches as tasks of one persistent launch (fgk_tasks.cu). Every
- * task is a tile of at most FGK_TASK_POINTS points:
+ * task is a tile of at most fgk_tasks_points() points:
  *   SMALL  n same-size items (whole transforms, tg threads each);
  *   COLS   lanes of columns of a big item's four-step split L = L1 L2 (DFTs
  *          of length L1 from the input, twiddled, into the item's scratch);
  *   ROWS   lanes of rows of that scratch (DFTs of length L2 into the
  *          output); they start once every COLS tile of the item is done. */
-#define FGK_TASK_POINTS 4096
+
 enum fgk_task_kind { FGK_TASK_SMALL = 0, FGK_TASK_COLS = 1, FGK_TASK_ROWS = 2 };
 
 typedef struct fgk_task {
@@ -137,10 +137,14 @@ int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in,
  * when a bounded wait gives up */
 int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                         const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig, int *counters_dev,
-                        float *scratch_dev, int op, const float *in_base, float *out_base, int num_sms,
-                        int *err_flag, void *stream);
+                        float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
+                        int num_sms, int *err_flag, void *stream);
 int    fgk_tasks_grid(int num_sms);
 int    fgk_tasks_threads(void);
+/* points of a tile (items up to this size run whole) and the shared-memory
+ * slots of one of its two buffers */
+int    fgk_tasks_points(void);
+int    fgk_tasks_slots(void);
 
 /* Static (compile-time) kernels, fgk_static*.cu: `fgk_static_count`
  * variants exist for (modulation, L); fgk_static_info describes variant v

@@ -1,15 +1,15 @@
 /* Ragged batches as one persistent launch of tile tasks.
  *
- * Every task is a tile of at most FGK_TASK_POINTS points held in two padded
+ * Every task is a tile of at most FGKT_POINTS points held in two padded
  * shared-memory buffers (ping-pong Stockham stages, one butterfly per thread
  * at a time, runtime radix; fgk_pingpong.cuh), so one CTA of 256 threads
  * needs 70 KB and three CTAs share an SM: while one loads its tile from HBM
  * the others compute, which is what keeps enough bytes in flight. Loads are
  * issued eight per thread before any is used.
  *
- *   SMALL  n items of one size L <= FGK_TASK_POINTS, whole transforms side
+ *   SMALL  n items of one size L <= FGKT_POINTS, whole transforms side
  *          by side (tg threads each), HBM in, HBM out.
- *   COLS   a big item (L > FGK_TASK_POINTS) split L = L1 L2 (the fftset's
+ *   COLS   a big item (L > FGKT_POINTS) split L = L1 L2 (the fftset's
  *          four-step plan: n = L2 n1 + n2, k = k1 + L1 k2): 2^ls1 adjacent
  *          columns n2, each a DFT of length L1 over n1 whose first stage
  *          reads the input directly (row segments of 2^ls1 elements) and
@@ -41,6 +41,9 @@
 
 namespace fgk {
 
+#ifndef FGKT_POINTS
+#define FGKT_POINTS 4096 /* points of a tile */
+#endif
 #ifndef FGKT_THREADS
 #define FGKT_THREADS 256 /* threads of a task CTA */
 #endif
@@ -48,7 +51,8 @@ namespace fgk {
 #define FGKT_MIN_CTAS 3 /* resident CTAs per SM the registers are budgeted for */
 #endif
 constexpr int TK_THREADS = FGKT_THREADS;
-constexpr int TK_SLOTS = FGK_TASK_POINTS + FGK_TASK_POINTS / 16 + 1; /* rslots(FGK_TASK_POINTS) */
+/* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
+constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
 constexpr uint32_t TK_SPIN_LIMIT = 1u << 22;                         /* x 256 ns: about a second */
 
 /* q = w / d for 0 <= w < 2^24, inv = 1/d (one correction step) */
@@ -98,22 +102,42 @@ __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int L
 /* First stage of a tile (ns = 1, no twiddles) straight from memory:
  * butterfly j of lane l reads ld(j + p nbf, l) (lanes fastest, so a warp
  * reads consecutive lanes of one element: the row segments in memory). */
+/* butterflies a thread loads side by side in the first stage, so that
+ * 16 loads are in flight for the radices 2, 4 and 8 */
+template <int R> struct Batch {
+	static constexpr int B = 1;
+};
+
 template <int R, class Ld>
 __device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls, int tid, int T)
 {
+	constexpr int B = Batch<R>::B;
 	const int nbf = Lp / R;
 	const int items = nbf << ls;
 	const int lm = (1 << ls) - 1;
-	for (int w = tid; w < items; w += T) {
-		const int j = w >> ls, lane = w & lm;
-		float2 v[R];
+	for (int w0 = tid; w0 < items; w0 += B * T) {
+		float2 v[B][R];
 #pragma unroll
-		for (int p = 0; p < R; p++)
-			v[p] = ld(j + p * nbf, lane);
-		Radix<R>::run(v);
+		for (int b = 0; b < B; b++) {
+			const int w = w0 + b * T;
+			if (w < items) {
+				const int j = w >> ls, lane = w & lm;
 #pragma unroll
-		for (int q = 0; q < R; q++)
-			dst[rslot(((j * R + q) << ls) + lane)] = v[q];
+				for (int p = 0; p < R; p++)
+					v[b][p] = ld(j + p * nbf, lane);
+			}
+		}
+#pragma unroll
+		for (int b = 0; b < B; b++) {
+			const int w = w0 + b * T;
+			if (w < items) {
+				const int j = w >> ls, lane = w & lm;
+				Radix<R>::run(v[b]);
+#pragma unroll
+				for (int q = 0; q < R; q++)
+					dst[rslot(((j * R + q) << ls) + lane)] = v[b][q];
+			}
+		}
 	}
 }
 
@@ -215,14 +239,13 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 /* n items of one size, tg threads each (group g = threadIdx / tg), each
  * group's first stage reading its item and its last stage writing its
  * output directly. */
+template <bool inverse, bool freq>
 __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *__restrict__ plans,
-                                           const fgk_rg_item *__restrict__ items, int op, const float *in_base,
+                                           const fgk_rg_item *__restrict__ items, const float *in_base,
                                            float *out_base, float2 *smem)
 {
 	const fgk_plan *pl = plans + tk.ref;
 	const int L = (int)pl->L;
-	const bool freq = pl->modulation == FGK_MOD_FREQOFF;
-	const bool inverse = op == FGK_OP_INVERSE;
 	const int n = (int)(tk.b & 0xffff), T = (int)(tk.b >> 16);
 	const int g = (int)threadIdx.x / T;
 	const int tid = (int)threadIdx.x - g * T;
@@ -269,17 +292,16 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
  * input into the item's scratch, which is laid out by ROWS tiles: element
  * (k1, n2) at ((k1 >> ls2) L2 + n2) 2^ls2 + (k1 & (2^ls2 - 1)), so a ROWS
  * tile reads one contiguous block with its lanes fastest. */
-__device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, int op, const float *in_base,
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, const float *in_base,
                                           float2 *scratch, int *done, float2 *smem)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
-	const uint64_t L = (uint64_t)L1 * L2;
+	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
 	const int ls = (int)bg.ls1;
 	const int ls2 = (int)bg.ls2, lm2 = (1 << ls2) - 1;
 	const int n2base = (int)(tk.a << ls);
-	const bool freq = p->modulation == FGK_MOD_FREQOFF;
-	const bool inverse = op == FGK_OP_INVERSE;
 	const float *x = in_base + bg.in_off;
 	const float2 *x2 = reinterpret_cast<const float2 *>(x);
 	const float2 *m1 = (const float2 *)p->m1, *m2 = (const float2 *)p->m2;
@@ -290,7 +312,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 		const int n2 = n2base + lane;
 		if (n2 >= L2)
 			return make_float2(0.f, 0.f);
-		const uint64_t n = (uint64_t)n1 * L2 + n2;
+		const uint32_t n = (uint32_t)n1 * (uint32_t)L2 + (uint32_t)n2;
 		if (!inverse) {
 			if (freq)
 				return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), cmul(__ldg(m1 + n1), __ldg(m2 + n2)));
@@ -306,29 +328,31 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 			return;
 		const uint32_t m = (uint32_t)n2 * (uint32_t)k1;
 		const float2 w = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
-		__stcg(S + (((uint64_t)(k1 >> ls2) * L2 + n2) << ls2) + (k1 & lm2), cmul(v, w));
+		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
+		       cmul(v, w));
 	};
 	tile_chain<true>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                 (int)blockDim.x, true, ld, st, [] {});
-	__threadfence();
+	/* the CTA's scratch stores, then one gpu-scope release of the count */
 	__syncthreads();
-	if (threadIdx.x == 0)
+	if (threadIdx.x == 0) {
+		__threadfence();
 		atomicAdd(done, 1);
+	}
 }
 
 /* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
  * into X[k1 + L1 k2] */
-__device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, int op, float *out_base,
-                                          float2 *scratch, const int *done, int *err, float2 *smem, int *failed)
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, float *out_base, float2 *scratch,
+                                          const int *done, int *err, float2 *smem, int *failed)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
-	const uint64_t L = (uint64_t)L1 * L2;
+	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
 	const int ls = (int)bg.ls2, nl = 1 << ls;
 	const int k1base = (int)(tk.a << ls);
 	const int nrow = min(nl, L1 - k1base);
-	const bool freq = p->modulation == FGK_MOD_FREQOFF;
-	const bool inverse = op == FGK_OP_INVERSE;
 	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
 
 	/* every COLS tile of this item, bounded */
@@ -359,12 +383,12 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 	float *o = out_base + bg.out_off;
 	float2 *o2 = reinterpret_cast<float2 *>(o);
 	const float2 *q1 = (const float2 *)p->n1, *q2 = (const float2 *)p->n2;
-	auto ld = [&](int n2, int lane) { return __ldcg(Stile + ((uint64_t)n2 << ls) + lane); };
+	auto ld = [&](int n2, int lane) { return __ldcg(Stile + (((uint32_t)n2 << ls) + (uint32_t)lane)); };
 	auto st = [&](int k2, int lane, float2 v) {
 		if (lane >= nrow)
 			return;
 		const int k1 = k1base + lane;
-		const uint64_t m = (uint64_t)k1 + (uint64_t)L1 * k2;
+		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * (uint32_t)k2;
 		if (!inverse) {
 			if (!freq)
 				__stcs(o2 + m, v);
@@ -392,11 +416,13 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 }
 
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the
- * current one starts, so the claim's round trip overlaps the work. */
+ * current one starts, so the claim's round trip overlaps the work. One
+ * instantiation per (direction, modulation): a batch has one of each. */
+template <bool inverse, bool freq>
 __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs, int *counters,
-                float2 *scratch, int op, const float *in_base, float *out_base, int *err)
+                float2 *scratch, const float *in_base, float *out_base, int *err)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
@@ -417,11 +443,12 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 		if (threadIdx.x == 0)
 			ahead = (uint32_t)atomicAdd(counters, 1);
 		if (tk.kind == FGK_TASK_SMALL)
-			task_small(tk, plans, items, op, in_base, out_base, smem);
+			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem);
 		else if (tk.kind == FGK_TASK_COLS)
-			task_cols(tk, bigs[tk.ref], op, in_base, scratch, counters + 1 + tk.ref, smem);
+			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem);
 		else
-			task_rows(tk, bigs[tk.ref], op, out_base, scratch, counters + 1 + tk.ref, err, smem, &failed);
+			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, smem,
+			                         &failed);
 		__syncthreads(); /* buffers are reused by the next task */
 		if (threadIdx.x == 0) {
 			cur = ahead;
@@ -433,6 +460,16 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 }
 
 } /* namespace fgk */
+
+extern "C" int fgk_tasks_points(void)
+{
+	return FGKT_POINTS;
+}
+
+extern "C" int fgk_tasks_slots(void)
+{
+	return fgk::TK_SLOTS;
+}
 
 extern "C" int fgk_tasks_threads(void)
 {
@@ -446,16 +483,18 @@ extern "C" int fgk_tasks_grid(int num_sms)
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
-                                int *counters_dev, float *scratch_dev, int op, const float *in_base, float *out_base,
-                                int num_sms, int *err_flag, void *stream)
+                                int *counters_dev, float *scratch_dev, int op, int modulation, const float *in_base,
+                                float *out_base, int num_sms, int *err_flag, void *stream)
 {
 	using namespace fgk;
 	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
+	const bool inv = op == FGK_OP_INVERSE, freq = modulation == FGK_MOD_FREQOFF;
+	auto k = inv ? (freq ? task_kernel<true, true> : task_kernel<true, false>)
+	             : (freq ? task_kernel<false, true> : task_kernel<false, false>);
 	cudaError_t e;
-	(void)bigs_dev;
 	if (ntasks == 0)
 		return 0;
-	if ((e = cudaFuncSetAttribute((const void *)task_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+	if ((e = cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
 	    cudaSuccess)
 		return (int)e;
 	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig), (cudaStream_t)stream)) != cudaSuccess)
@@ -463,8 +502,8 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms);
 	if (grid > ntasks)
 		grid = ntasks;
-	task_kernel<<<grid, TK_THREADS, smem, (cudaStream_t)stream>>>(tasks_dev, ntasks, plans_dev, items_dev, bigs_dev,
-	                                                              counters_dev, reinterpret_cast<float2 *>(scratch_dev),
-	                                                              op, in_base, out_base, err_flag);
+	k<<<grid, TK_THREADS, smem, (cudaStream_t)stream>>>(tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, counters_dev,
+	                                                    reinterpret_cast<float2 *>(scratch_dev), in_base, out_base,
+	                                                    err_flag);
 	return (int)cudaGetLastError();
 }
