@@ -8,8 +8,10 @@
  *   - larger items: their four-step split L = L1 L2, COLS tiles (columns
  *     into the item's scratch) then ROWS tiles (rows into the output). The
  *     ROWS tiles of item i are listed after the COLS tiles of item i + D,
- *     D chosen so that a full grid of tasks separates them, so ROWS tiles
- *     rarely wait.
+ *     D chosen so that two full grids of tasks separate them, so ROWS tiles
+ *     rarely wait. Big items need a split with both factors <= 256 (every
+ *     size up to 65536 bins has one); larger sizes are refused
+ *     (FFTSET_E_UNSUPPORTED) and run through the batched calls instead.
  * Big items come first (largest first), then the SMALL tasks (largest
  * first), which balances the tail. fftset_ragged_execute records the launch
  * into a CUDA graph on first use (and when the base pointers change) and
@@ -183,7 +185,8 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 				goto fail;
 			L1 = f->p4.L1;
 			L2 = f->p4.L2;
-			if (L1 > (uint32_t)fgk_tasks_points() || L2 > (uint32_t)fgk_tasks_points()) {
+			/* tiles of 16 or more lanes (the task kernel's Rows layout) */
+			if ((L1 << 4) > (uint32_t)fgk_tasks_points() || (L2 << 4) > (uint32_t)fgk_tasks_points()) {
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
 			}
@@ -211,7 +214,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	if (nbig) {
 		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms);
 		const uint64_t avg = (total_cols + nbig - 1) / nbig;
-		uint32_t D = (uint32_t)((grid + avg - 1) / avg) + 1, b, t;
+		uint32_t D = (uint32_t)((2 * grid + avg - 1) / avg) + 1, b, t;
 		for (b = 0; b < nbig + D; b++) {
 			if (b < nbig)
 				for (t = 0; t < bigs[b].ncols; t++)

@@ -19,6 +19,8 @@
  *          DFTs of length L2 over n2, the last stage writing X[k1 + L1 k2]
  *          directly (segments of 2^ls2 elements).
  * Only the middle stages of a big-item tile go through shared memory.
+ * Big-item tiles have at least 16 lanes (L1, L2 <= 256), which makes the
+ * Rows layout below conflict-free.
  *
  * A ROWS task waits for all COLS tasks of its item: each COLS task bumps the
  * item's counter after its stores are visible (threadfence), and a ROWS task
@@ -67,12 +69,27 @@ __device__ __forceinline__ int tk_div(int w, int d, float inv)
 	return q;
 }
 
+/* Shared-memory layouts of a tile (element i of lane l):
+ *   Pad   (one lane, whole items)  slot i + i/16: the strided accesses of a
+ *         stage spread over the banks;
+ *   Rows  (16 or more lanes)       slot i (nl + 1) + l: linear in i, so a
+ *         stage's R accesses are one base plus multiples of a stride, and
+ *         conflict-free whether a warp runs along the lanes or along i. */
+struct Pad {
+	int ls;
+	__device__ __forceinline__ int slot(int i, int lane) const { return rslot((i << ls) + lane); }
+};
+struct Rows {
+	int ls;
+	__device__ __forceinline__ int slot(int i, int lane) const { return i * ((1 << ls) + 1) + lane; }
+};
+
 /* Stockham stage over a lane-interleaved tile: element i of lane l at
  * rslot((i << ls) + l); work item w = (butterfly j, lane) with the lane
  * fastest, so a warp's accesses are consecutive slots. */
-template <int R>
+template <int R, class A>
 __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int Lp, int ls, int ns,
-                                           const float2 *__restrict__ tw, int tid, int T)
+                                           const float2 *__restrict__ tw, int tid, int T, A ad)
 {
 	const int nbf = Lp / R;
 	const int items = nbf << ls;
@@ -82,7 +99,7 @@ __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int L
 		float2 v[R];
 #pragma unroll
 		for (int p = 0; p < R; p++)
-			v[p] = src[rslot(((j + p * nbf) << ls) + lane)];
+			v[p] = src[ad.slot(j + p * nbf, lane)];
 		const int k = j % ns;
 		if (ns > 1) {
 			const float2 *t = tw + k * (R - 1);
@@ -94,7 +111,7 @@ __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int L
 		const int base = (j - k) * R + k;
 #pragma unroll
 		for (int q = 0; q < R; q++)
-			dst[rslot(((base + q * ns) << ls) + lane)] = v[q];
+			dst[ad.slot(base + q * ns, lane)] = v[q];
 	}
 }
 
@@ -108,8 +125,8 @@ template <int R> struct Batch {
 	static constexpr int B = 1;
 };
 
-template <int R, class Ld>
-__device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls, int tid, int T)
+template <int R, class A, class Ld>
+__device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls, int tid, int T, A ad)
 {
 	constexpr int B = Batch<R>::B;
 	const int nbf = Lp / R;
@@ -135,7 +152,7 @@ __device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls,
 				Radix<R>::run(v[b]);
 #pragma unroll
 				for (int q = 0; q < R; q++)
-					dst[rslot(((j * R + q) << ls) + lane)] = v[b][q];
+					dst[ad.slot(j * R + q, lane)] = v[b][q];
 			}
 		}
 	}
@@ -145,9 +162,9 @@ __device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls,
  * outputs j + q nbf) straight to memory through st(k, lane, v). JF: a warp
  * takes consecutive butterflies j of one lane (consecutive outputs k),
  * otherwise consecutive lanes of one butterfly. */
-template <int R, bool JF, class St>
+template <int R, bool JF, class A, class St>
 __device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, int ls, const float2 *__restrict__ tw,
-                                          int tid, int T)
+                                          int tid, int T, A ad)
 {
 	const int nbf = Lp / R;
 	const int items = nbf << ls;
@@ -165,7 +182,7 @@ __device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, in
 		float2 v[R];
 #pragma unroll
 		for (int p = 0; p < R; p++)
-			v[p] = src[rslot(((j + p * nbf) << ls) + lane)];
+			v[p] = src[ad.slot(j + p * nbf, lane)];
 		if (nbf > 1) {
 			const float2 *t = tw + j * (R - 1);
 #pragma unroll
@@ -200,11 +217,12 @@ __device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, i
  * memory (A/B ping-pong), last stage to st. `after_first` runs once the first
  * stage is done (all of its reads have returned). Threads with active ==
  * false only take part in the barriers. */
-template <bool JF, class Ld, class St, class After>
+template <bool JF, class AD, class Ld, class St, class After>
 __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw, int Lp, int ls, float2 *A,
                                            float2 *B, int tid, int T, bool active, Ld &&ld, St &&st,
                                            After &&after_first)
 {
+	const AD ad{ls};
 	const int n = (int)ch->nstages;
 	if (n == 1) {
 		if (active)
@@ -215,7 +233,7 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	}
 	if (active) {
 		const fgk_stage st0 = ch->st[0];
-		FGKR_RADIX_SWITCH(st0.radix, (lane_first<R_>(ld, A, Lp, ls, tid, T)));
+		FGKR_RADIX_SWITCH(st0.radix, (lane_first<R_>(ld, A, Lp, ls, tid, T, ad)));
 	}
 	__syncthreads();
 	after_first();
@@ -223,7 +241,7 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	for (int s = 1; s < n - 1; s++) {
 		const fgk_stage sm = ch->st[s];
 		if (active)
-			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tw + sm.tw_off, tid, T)));
+			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tw + sm.tw_off, tid, T, ad)));
 		__syncthreads();
 		float2 *t = src;
 		src = dst;
@@ -231,7 +249,7 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	}
 	if (active) {
 		const fgk_stage sl = ch->st[n - 1];
-		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tw + sl.tw_off, tid, T)));
+		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tw + sl.tw_off, tid, T, ad)));
 	}
 }
 
@@ -285,7 +303,8 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 			__stcs(y2 + k, conjf2(v));
 		}
 	};
-	tile_chain<false>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st, [] {});
+	tile_chain<false, Pad>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
+	                       [] {});
 }
 
 /* COLS: columns n2base .. n2base + 2^ls1 - 1, DFTs of length L1 from the
@@ -331,8 +350,8 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
 		       cmul(v, w));
 	};
-	tile_chain<true>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                 (int)blockDim.x, true, ld, st, [] {});
+	tile_chain<true, Rows>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                       (int)blockDim.x, true, ld, st, [] {});
 	/* the CTA's scratch stores, then one gpu-scope release of the count */
 	__syncthreads();
 	if (threadIdx.x == 0) {
@@ -412,7 +431,8 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		for (uintptr_t a = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)tid * 128; a + 128 <= b1; a += (uintptr_t)T * 128)
 			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
 	};
-	tile_chain<false>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st, discard);
+	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
+	                        discard);
 }
 
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the

@@ -82,3 +82,6 @@ def test_ragged_rejects_bad_input(fftset_lib, gpu_set):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 7], [0, 200], [0, 200])
     with pytest.raises(fftset_lib.FftsetError):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64], [1], [0])
+    # items beyond 65536 bins have no split with both factors <= 256
+    with pytest.raises(fftset_lib.FftsetError):
+        fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 131072], [0, 128], [0, 128])
