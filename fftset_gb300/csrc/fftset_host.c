@@ -162,7 +162,7 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 	fgk_plan4 *p = &f->p4;
 	const unsigned L = f->lfft;
 	const uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
-	size_t n1, n2, nhi, nlo, off[10], total, i;
+	size_t n1, n2, nhi, nlo, off[11], total, i;
 	float *h = NULL;
 	char *d = NULL;
 	int32_t *kidx = NULL;
@@ -183,18 +183,22 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		p->tshift++;
 	nlo = (size_t)1 << p->tshift;
 	nhi = (L + nlo - 1) / nlo;
-	/* float2 counts: tw1, tw2, thi, tlo, m1, m2, n1, n2; then kidx (int32) and the plan copy */
+	/* w_{R L2}^m for the task kernel's inter-step twiddle, R the last radix of
+	 * the column chain */
+	p->nq = p->c1.st[p->c1.nstages - 1].radix * p->L2;
+	/* float2 counts: tw1, tw2, thi, tlo, m1, m2, n1, n2, tq; then kidx (int32) and the plan copy */
 	{
-		const size_t cnt[8] = {n1 ? n1 : 1, n2 ? n2 : 1, nhi, nlo, p->L1, p->L2, p->L1, p->L2};
+		const size_t cnt[9] = {n1 ? n1 : 1, n2 ? n2 : 1, nhi, nlo, p->L1, p->L2, p->L1, p->L2, p->nq};
 		total = fs_align(sizeof(fgk_plan4));
-		for (i = 0; i < 8; i++) {
+		for (i = 0; i < 9; i++) {
 			off[i] = total;
 			total += fs_align(cnt[i] * 2 * sizeof(float));
 		}
-		off[8] = total;
+		off[9] = total;
 		total += fs_align(sizeof(int32_t) * L);
 	}
-	h = (float *)malloc(sizeof(float) * 2 * (n1 + n2 + nhi + nlo + 2 * (size_t)p->L1 + 2 * (size_t)p->L2 + 2));
+	h = (float *)malloc(sizeof(float) * 2 *
+	                    (n1 + n2 + nhi + nlo + 2 * (size_t)p->L1 + 2 * (size_t)p->L2 + (size_t)p->nq + 2));
 	kidx = (int32_t *)malloc(sizeof(int32_t) * L);
 	if (!h || !kidx)
 		goto out;
@@ -209,7 +213,7 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 	}
 	{
 		float *w = h;
-		float *tw1 = w, *tw2, *thi, *tlo, *m1, *m2, *q1, *q2;
+		float *tw1 = w, *tw2, *thi, *tlo, *m1, *m2, *q1, *q2, *tq;
 		size_t k;
 		fgk_chain_twiddles(&p->c1, tw1);
 		tw2 = tw1 + 2 * (n1 ? n1 : 1);
@@ -220,6 +224,12 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		m2 = m1 + 2 * (size_t)p->L1;
 		q1 = m2 + 2 * (size_t)p->L2;
 		q2 = q1 + 2 * (size_t)p->L1;
+		tq = q2 + 2 * (size_t)p->L2;
+		for (k = 0; k < p->nq; k++) {
+			double a = -2.0 * M_PI * (double)k / (double)p->nq;
+			tq[2 * k] = (float)cos(a);
+			tq[2 * k + 1] = (float)sin(a);
+		}
 		for (k = 0; k < nhi; k++) {
 			double a = -2.0 * M_PI * (double)(k * nlo) / (double)L;
 			thi[2 * k] = (float)cos(a);
@@ -245,10 +255,10 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 			q2[2 * k + 1] = (float)sin(b);
 		}
 		{
-			float *srcs[8] = {tw1, tw2, thi, tlo, m1, m2, q1, q2};
-			const size_t cnt[8] = {n1, n2, nhi, nlo, p->L1, p->L2, p->L1, p->L2};
-			const void **dst[8] = {&p->tw1, &p->tw2, &p->thi, &p->tlo, &p->m1, &p->m2, &p->n1, &p->n2};
-			for (k = 0; k < 8; k++) {
+			float *srcs[9] = {tw1, tw2, thi, tlo, m1, m2, q1, q2, tq};
+			const size_t cnt[9] = {n1, n2, nhi, nlo, p->L1, p->L2, p->L1, p->L2, p->nq};
+			const void **dst[9] = {&p->tw1, &p->tw2, &p->thi, &p->tlo, &p->m1, &p->m2, &p->n1, &p->n2, &p->tq};
+			for (k = 0; k < 9; k++) {
 				*dst[k] = d + off[k];
 				if (cnt[k] &&
 				    (e = cudaMemcpy(d + off[k], srcs[k], cnt[k] * 2 * sizeof(float), cudaMemcpyHostToDevice)) !=
@@ -258,10 +268,10 @@ int fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f)
 		}
 	}
 	p->dev = (const fgk_plan4 *)d;
-	if ((e = cudaMemcpy(d + off[8], kidx, sizeof(int32_t) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+	if ((e = cudaMemcpy(d + off[9], kidx, sizeof(int32_t) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
 	    (e = cudaMemcpy(d, p, sizeof(fgk_plan4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		goto cuda_fail;
-	f->kidx4 = (const int32_t *)(d + off[8]);
+	f->kidx4 = (const int32_t *)(d + off[9]);
 	f->dmem4 = d;
 	rc = FFTSET_OK;
 	goto out;

@@ -74,6 +74,8 @@ typedef struct fgk_plan4 {
 	const void *thi, *tlo;
 	const void *m1, *m2;        /* e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2L)}: input modulation */
 	const void *n1, *n2;        /* e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2)}: output modulation */
+	uint32_t    nq;             /* R L2, R the last radix of c1 */
+	const void *tq;             /* w_{R L2}^m, m < nq */
 	const struct fgk_plan4 *dev;
 } fgk_plan4;
 

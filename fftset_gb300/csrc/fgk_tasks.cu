@@ -159,7 +159,7 @@ __device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls,
 }
 
 /* Last stage of a tile (ns = Lp/R: butterfly j twiddled by w^{p j},
- * outputs j + q nbf) straight to memory through st(k, lane, v). JF: a warp
+ * outputs k = j + q nbf) straight to memory through st(j, q, nbf, lane, v). JF: a warp
  * takes consecutive butterflies j of one lane (consecutive outputs k),
  * otherwise consecutive lanes of one butterfly. */
 template <int R, bool JF, class A, class St>
@@ -192,7 +192,7 @@ __device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, in
 		Radix<R>::run(v);
 #pragma unroll
 		for (int q = 0; q < R; q++)
-			st(j + q * nbf, lane, v[q]);
+			st(j, q, nbf, lane, v[q]);
 	}
 }
 
@@ -209,7 +209,7 @@ __device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, i
 		Radix<R>::run(v);
 #pragma unroll
 		for (int q = 0; q < R; q++)
-			st(q, lane, v[q]);
+			st(0, q, 1, lane, v[q]);
 	}
 }
 
@@ -287,7 +287,8 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 			return i < hc ? conjf2(__ldcs(X + 2 * i)) : __ldcs(X + 2 * (L - 1 - i) + 1);
 		return conjf2(__ldcs(X + i));
 	};
-	auto st = [&](int k, int, float2 v) {
+	auto st = [&](int j, int q, int nbf, int, float2 v) {
+		const int k = j + q * nbf;
 		if (!inverse) {
 			if (!freq)
 				__stcs(y2 + k, v);
@@ -341,12 +342,17 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
 		return conjf2(__ldcs(x2 + n));
 	};
-	auto st = [&](int k1, int lane, float2 v) {
+	const float2 *tq = (const float2 *)p->tq;
+	/* w_L^{n2 k1}, k1 = j + q nbf: w_L^{n2 j} w_{R L2}^{n2 q} (L = R nbf L2;
+	 * n2 q < R L2, so no reduction) */
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
 		const int n2 = n2base + lane;
 		if (n2 >= L2)
 			return;
-		const uint32_t m = (uint32_t)n2 * (uint32_t)k1;
-		const float2 w = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const int k1 = j + q * nbf;
+		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
+		const float2 a = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 w = q ? cmul(a, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : a;
 		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
 		       cmul(v, w));
 	};
@@ -403,9 +409,10 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 	float2 *o2 = reinterpret_cast<float2 *>(o);
 	const float2 *q1 = (const float2 *)p->n1, *q2 = (const float2 *)p->n2;
 	auto ld = [&](int n2, int lane) { return __ldcg(Stile + (((uint32_t)n2 << ls) + (uint32_t)lane)); };
-	auto st = [&](int k2, int lane, float2 v) {
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
 		if (lane >= nrow)
 			return;
+		const int k2 = j + q * nbf;
 		const int k1 = k1base + lane;
 		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * (uint32_t)k2;
 		if (!inverse) {
