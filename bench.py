@@ -528,6 +528,32 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def profile_case(args):
+    """A small fixed case of one workload for ncu captures (no timing, no
+    JSON line): `ragged` = the first --items items of the ragged draw, one
+    launch per execute (no graph), executed three times."""
+    import torch
+    import fftset_gb300 as fs
+    if args.profile == "ragged":
+        sizes = [int(v) for v in ragged_sizes(20000, 4)[:args.items]]
+        offs, o = [], 0
+        for v in sizes:
+            offs.append(o)
+            o += 2 * v
+        S = fs.FftSet()
+        S.set_stream(torch.cuda.current_stream())
+        S.set_blocking(False)
+        x = torch.from_numpy(np.random.default_rng(5).uniform(-1, 1, o).astype(np.float32)).cuda()
+        y = torch.empty_like(x)
+        rb = fs.Ragged(S, fs.COMPLEX, fs.OP_FORWARD, sizes, offs, offs)
+        rb.set_graph(False)
+        for _ in range(3):
+            rb.execute(y, x)
+        torch.cuda.synchronize()
+        S.check()
+        print(json.dumps({"profile": "ragged", "items": len(sizes), "bytes": rb.bytes}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -538,8 +564,13 @@ def main():
                     help="only the headline workload (no per-call, ragged, large and adjoint lines)")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin the conv kernel variant (-1 generic) instead of autotuning")
+    ap.add_argument("--profile", choices=["ragged"], default=None,
+                    help="run one small fixed case for an ncu capture instead of the benchmark")
+    ap.add_argument("--items", type=int, default=2000, help="items of the --profile ragged case")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -100,6 +100,24 @@ int fftset_init(struct fftset *fc)
 		return -1;
 	}
 	*fs->host_flag = 0;
+	{
+		int p, ok = cudaEventCreateWithFlags(&fs->pipe_ev, cudaEventDisableTiming) == cudaSuccess;
+		for (p = 0; p < FS_PIPE && ok; p++)
+			ok = cudaStreamCreateWithFlags(&fs->pipe[p], cudaStreamNonBlocking) == cudaSuccess;
+		if (!ok) {
+			cudaGetLastError();
+			for (p = 0; p < FS_PIPE; p++)
+				if (fs->pipe[p])
+					cudaStreamDestroy(fs->pipe[p]);
+			if (fs->pipe_ev)
+				cudaEventDestroy(fs->pipe_ev);
+			cudaFreeHost(fs->host_flag);
+			pthread_mutex_destroy(&fs->lock);
+			cudaStreamDestroy(fs->own_stream);
+			free(fs);
+			return -1;
+		}
+	}
 	fs->stream = fs->own_stream;
 	fs->blocking = 1;
 	fs->layout_vw = 4;
@@ -124,6 +142,11 @@ void fftset_destroy(struct fftset *fc)
 		cudaFree(p->dmem4);
 		free(p);
 	}
+	for (i = 0; i < FS_PIPE; i++) {
+		cudaStreamSynchronize(fs->pipe[i]);
+		cudaStreamDestroy(fs->pipe[i]);
+	}
+	cudaEventDestroy(fs->pipe_ev);
 	for (i = 0; i < FS_NSTAGE; i++)
 		cudaFree(fs->stage[i]);
 	cudaStreamDestroy(fs->own_stream);
@@ -502,27 +525,26 @@ int fs_check_flag(struct fs_impl *fs)
 #define FS_STATIC_MIN_COUNT 64
 
 static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *out, const float *in,
-                             const float *kern, unsigned count, size_t in_stride, size_t out_stride)
+                             const float *kern, unsigned count, size_t in_stride, size_t out_stride,
+                             cudaStream_t stream)
 {
 	struct fs_impl *fs = f->fs;
 	if (v >= 0 && v < f->nvar) {
-		int rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, fs->stream,
+		int rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, stream,
 		                           fs->num_sms, fs->dev_flag);
 		if (rc >= 0)
 			return rc;
 		/* the variant cannot take these buffers (alignment): any other
 		 * compiled variant that can, else the generic kernel */
 		for (v = 0; v < f->nvar; v++) {
-			rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, fs->stream,
+			rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, stream,
 			                       fs->num_sms, fs->dev_flag);
 			if (rc >= 0)
 				return rc;
 		}
 	}
-	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, fs->stream);
+	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, stream);
 }
-
-
 
 int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
                      unsigned count, size_t in_stride, size_t out_stride)
@@ -540,7 +562,90 @@ int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, c
 		                           count, in_stride ? in_stride : nf, out_stride ? out_stride : nf, nf, fs->stream);
 	}
 	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
-	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride);
+	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride, f->fs->stream);
+}
+
+/* m rows of nf floats, `stride` floats apart on both sides: only the rows
+ * move (the caller's memory between rows is left alone) */
+static cudaError_t fs_copy_rows(float *dst, const float *src, size_t stride, size_t nf, size_t m,
+                                enum cudaMemcpyKind kind, cudaStream_t st)
+{
+	if (m == 1 || stride == nf)
+		return cudaMemcpyAsync(dst, src, ((m - 1) * stride + nf) * sizeof(float), kind, st);
+	return cudaMemcpy2DAsync(dst, stride * sizeof(float), src, stride * sizeof(float), nf * sizeof(float), m, kind,
+	                         st);
+}
+
+/* Host buffers, many blocks: chunks of about FS_CHUNK_BYTES go round-robin
+ * over FS_PIPE streams, each chunk copied in, transformed and copied out on
+ * its stream, so that the copies in both directions and the kernels of
+ * different chunks overlap. Resident sizes only (the four-step passes share
+ * one work buffer). Called with fs->lock held; returns after the results are
+ * in `out`. */
+#define FS_CHUNK_BYTES ((size_t)16 << 20)
+
+static int fs_exec_pipelined(const struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in,
+                             size_t in_stride, const float *dkern, unsigned count, int in_dev, int out_dev)
+{
+	struct fs_impl *fs = f->fs;
+	const size_t nf = 2 * (size_t)f->lfft;
+	const size_t cb = FS_CHUNK_BYTES / (nf * sizeof(float)) ? FS_CHUNK_BYTES / (nf * sizeof(float)) : 1;
+	const size_t in_span = (cb - 1) * in_stride + nf, out_span = (cb - 1) * out_stride + nf;
+	float *sin = NULL, *sout = NULL;
+	size_t c, first;
+	int rc = FFTSET_OK, p;
+	cudaError_t e;
+
+	if (!in_dev) {
+		if ((rc = fs_stage_reserve(fs, 0, FS_PIPE * in_span * sizeof(float))) != 0)
+			return rc;
+		sin = (float *)fs->stage[0];
+	}
+	if (!out_dev) {
+		if ((rc = fs_stage_reserve(fs, 1, FS_PIPE * out_span * sizeof(float))) != 0)
+			return rc;
+		sout = (float *)fs->stage[1];
+	}
+	/* after everything already on the fftset's stream (the kernel-buffer copy) */
+	if ((e = cudaEventRecord(fs->pipe_ev, fs->stream)) != cudaSuccess)
+		return fs_cuda(fs, e);
+	for (p = 0; p < FS_PIPE; p++)
+		if ((e = cudaStreamWaitEvent(fs->pipe[p], fs->pipe_ev, 0)) != cudaSuccess)
+			return fs_cuda(fs, e);
+	for (c = 0, first = 0; first < count; c++, first += cb) {
+		const unsigned m = (unsigned)(count - first < cb ? count - first : cb);
+		cudaStream_t st = fs->pipe[c % FS_PIPE];
+		const float *din = in + first * in_stride;
+		float *dout = out + first * out_stride;
+		const int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1; /* the kernel the whole batch would use */
+		if (!in_dev) {
+			din = sin + (c % FS_PIPE) * in_span;
+			if ((e = fs_copy_rows((float *)din, in + first * in_stride, in_stride, nf, m, cudaMemcpyHostToDevice,
+			                      st)) != cudaSuccess) {
+				rc = fs_cuda(fs, e);
+				break;
+			}
+		}
+		if (!out_dev)
+			dout = sout + (c % FS_PIPE) * out_span;
+		if ((rc = fs_launch_variant(f, v, op, dout, din, dkern, m, in_stride, out_stride, st)) != 0) {
+			rc = rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
+			break;
+		}
+		if (!out_dev && (e = fs_copy_rows(out + first * out_stride, dout, out_stride, nf, m, cudaMemcpyDeviceToHost,
+		                                  st)) != cudaSuccess) {
+			rc = fs_cuda(fs, e);
+			break;
+		}
+	}
+	for (p = 0; p < FS_PIPE; p++) {
+		const int r = fs_cuda(fs, cudaStreamSynchronize(fs->pipe[p]));
+		if (rc == FFTSET_OK)
+			rc = r;
+	}
+	if (rc == FFTSET_OK)
+		rc = fs_check_flag(fs);
+	return rc;
 }
 
 /* Runs op on `count` blocks. Buffers of any memory kind. */
@@ -588,11 +693,28 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 	/* host buffers: stage through device memory */
 	pthread_mutex_lock(&fs->lock);
 	staged = 1;
+	if (!f->fourstep && count > 1 && count * nf * sizeof(float) >= 2 * FS_CHUNK_BYTES &&
+	    in_stride >= nf && out_stride >= nf) {
+		if (kern != NULL && !fs_is_device_ptr(kern)) {
+			if ((rc = fs_stage_reserve(fs, 2, nf * sizeof(float))))
+				goto done;
+			dkern = (const float *)fs->stage[2];
+			if ((e = cudaMemcpyAsync(fs->stage[2], kern, nf * sizeof(float), cudaMemcpyHostToDevice,
+			                         fs->stream)) != cudaSuccess) {
+				rc = fs_cuda(fs, e);
+				goto done;
+			}
+		}
+		rc = fs_exec_pipelined(f, op, out, out_stride, in, in_stride, dkern, count, fs_is_device_ptr(in),
+		                       fs_is_device_ptr(out));
+		goto done;
+	}
 	if (!fs_is_device_ptr(in)) {
 		if ((rc = fs_stage_reserve(fs, 0, in_span * sizeof(float))))
 			goto done;
 		din = (const float *)fs->stage[0];
-		if ((e = cudaMemcpyAsync(fs->stage[0], in, in_span * sizeof(float), cudaMemcpyHostToDevice, fs->stream)) !=
+		if ((e = fs_copy_rows((float *)fs->stage[0], in, count > 1 ? in_stride : nf, nf, count, cudaMemcpyHostToDevice,
+		                      fs->stream)) !=
 		    cudaSuccess) {
 			rc = fs_cuda(fs, e);
 			goto done;
@@ -619,7 +741,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		goto done;
 	}
 	if (dout != out) {
-		if ((e = cudaMemcpyAsync(out, dout, out_span * sizeof(float), cudaMemcpyDeviceToHost, fs->stream)) !=
+		if ((e = fs_copy_rows(out, dout, count > 1 ? out_stride : nf, nf, count, cudaMemcpyDeviceToHost, fs->stream)) !=
 		    cudaSuccess) {
 			rc = fs_cuda(fs, e);
 			goto done;
@@ -878,7 +1000,7 @@ int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, fl
 				rc = fs_cuda(fs, e);
 				goto done;
 			}
-			if ((rc = fs_launch_variant(f, v, op, out, in, kern, count, nf, nf)) != 0) {
+			if ((rc = fs_launch_variant(f, v, op, out, in, kern, count, nf, nf, fs->stream)) != 0) {
 				rc = fs_latch(fs, FFTSET_E_CUDA, rc);
 				goto done;
 			}

@@ -38,6 +38,7 @@ struct fftset_fft {
 };
 
 #define FS_NSTAGE 5 /* staging buffers: input, output, kernel, four-step work, adjoint scratch */
+#define FS_PIPE   3 /* streams of the host-buffer chunk pipeline */
 
 struct fs_impl {
 	cudaStream_t       stream;
@@ -55,6 +56,8 @@ struct fs_impl {
 	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
+	cudaStream_t       pipe[FS_PIPE]; /* host-buffer chunk pipeline (fs_exec) */
+	cudaEvent_t        pipe_ev;
 };
 
 

@@ -39,28 +39,34 @@ __device__ __forceinline__ void kg_bar(int g, int T)
 }
 
 /* natural-order input of the plan's forward chain: the block itself
- * (COMPLEX) or conj(x[i] + j x[L+i]) e^{-j pi i/(2L)} (FREQ_OFFSET_REAL) */
-__device__ __forceinline__ void kg_prologue(const fgk_plan *pl, float2 *buf, const float *x, int L, bool freq,
-                                            int tid, int T)
+ * (COMPLEX) or conj(x[i] + j x[L+i]) e^{-j pi i/(2L)} (FREQ_OFFSET_REAL);
+ * eight loads per thread in flight */
+template <bool FREQ>
+__device__ __forceinline__ void kg_prologue(const fgk_plan *pl, float2 *buf, const float *x, int L, int tid, int T)
 {
-	if (freq) {
+	if (FREQ) {
 		const float2 *mod = (const float2 *)pl->modtw;
-		for (int i = tid; i < L; i += T)
-			buf[rslot(i)] = cmul(make_float2(__ldcs(x + i), -__ldcs(x + L + i)), __ldg(mod + i));
+		batched_copy<8>(
+		    L, tid, T,
+		    [&](int i) { return cmul(make_float2(__ldcs(x + i), -__ldcs(x + L + i)), __ldg(mod + i)); },
+		    [&](int i, float2 v) { buf[rslot(i)] = v; });
 	} else {
 		const float2 *x2 = reinterpret_cast<const float2 *>(x);
-		for (int i = tid; i < L; i += T)
-			buf[rslot(i)] = __ldcs(x2 + i);
+		batched_copy<8>(
+		    L, tid, T, [&](int i) { return __ldcs(x2 + i); }, [&](int i, float2 v) { buf[rslot(i)] = v; });
 	}
 }
 
+/* Both blocks of a step (g_b into b0, x_b into b2) are loaded before either
+ * transform runs, so their loads overlap; g_b's chain then runs over b0/b1
+ * and x_b's over b2 and whichever of b0/b1 does not hold G_b. */
+template <bool FREQ>
 __global__ void __launch_bounds__(KG_THREADS, 1)
     kg_fused(const fgk_plan *__restrict__ pl, const float *gr, size_t g_stride, const float *x, size_t x_stride,
              uint32_t count, int T, int G, float2 *partials)
 {
 	extern __shared__ float2 smem[];
 	const int L = (int)pl->L;
-	const bool freq = pl->modulation == FGK_MOD_FREQOFF;
 	const int g = (int)threadIdx.x / T;
 	const int tid = (int)threadIdx.x - g * T;
 	const int slots = rslots(L);
@@ -74,13 +80,11 @@ __global__ void __launch_bounds__(KG_THREADS, 1)
 	auto sync = [&] { kg_bar(g, T); };
 	const uint64_t P = (uint64_t)gridDim.x * G;
 	for (uint64_t b = (uint64_t)blockIdx.x * G + g; b < count; b += P) {
-		kg_prologue(pl, b0, gr + b * g_stride, L, freq, tid, T);
+		kg_prologue<FREQ>(pl, b0, gr + b * g_stride, L, tid, T);
+		kg_prologue<FREQ>(pl, b2, x + b * x_stride, L, tid, T);
 		sync();
 		float2 *W = rg_chain(pl, b0, b1, true, tid, T, sync);
-		float2 *xa = W == b0 ? b1 : b0;
-		kg_prologue(pl, xa, x + b * x_stride, L, freq, tid, T);
-		sync();
-		const float2 *X = rg_chain(pl, xa, b2, true, tid, T, sync);
+		const float2 *X = rg_chain(pl, b2, W == b0 ? b1 : b0, true, tid, T, sync);
 #pragma unroll
 		for (int k = 0; k < KG_ACC; k++) {
 			const int i = tid + k * T;
@@ -171,11 +175,12 @@ extern "C" int fgk_launch_kgrad_fused(const fgk_plan *p, const float *grad_out, 
 	cudaError_t e;
 	if (!fgk_kgrad_fused_shape(p, &T, &G, &smem))
 		return (int)cudaErrorInvalidValue;
-	if ((e = cudaFuncSetAttribute((const void *)kg_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+	auto k = p->modulation == FGK_MOD_FREQOFF ? kg_fused<true> : kg_fused<false>;
+	if ((e = cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
 	    cudaSuccess)
 		return (int)e;
-	kg_fused<<<grid, T * G, smem, (cudaStream_t)stream>>>(p->dev, grad_out, g_stride, x, x_stride, count, (int)T,
-	                                                      (int)G, reinterpret_cast<float2 *>(partials));
+	k<<<grid, T * G, smem, (cudaStream_t)stream>>>(p->dev, grad_out, g_stride, x, x_stride, count, (int)T, (int)G,
+	                                               reinterpret_cast<float2 *>(partials));
 	return (int)cudaGetLastError();
 }
 

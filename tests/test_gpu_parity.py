@@ -419,3 +419,45 @@ def test_fourstep_large_single(gpu_set):
     r = torch.empty(2 * L, device="cuda")
     f.inverse(r, X)
     assert O.rel_l2(host(r) / L, x) <= tol(1, L)
+
+
+@pytest.mark.parametrize("mod,L,op", [(1, 1536, "conv"), (0, 1024, "forward"), (1, 4096, "inverse")])
+def test_host_buffers_chunk_pipeline(gpu_set, mod, L, op):
+    """Host (numpy) buffers large enough for the chunk pipeline (several
+    16 MB chunks over three streams), padded rows and in-place: the same
+    results as device buffers, every block written."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    B, pad = int(40e6 // (8 * L)), 6
+    rng = np.random.default_rng(L + 7)
+    x = rng.standard_normal((B, 2 * L + pad)).astype(np.float32)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    K = np.empty(2 * L, np.float32)
+    f.conv_get_kernel(K, h)
+    Kd = dev(K)
+    want = torch.empty(B, 2 * L, device="cuda")
+    xd = dev(x)[:, :2 * L].contiguous()
+    got = np.full((B, 2 * L + 2), np.nan, np.float32)
+    if op == "conv":
+        f.conv_batch(want, xd, Kd)
+        f.conv_batch(got, x, K)
+    elif op == "forward":
+        f.forward_batch(want, xd)
+        f.forward_batch(got, x)
+    else:
+        f.inverse_batch(want, xd)
+        f.inverse_batch(got, x)
+    w = host(want)
+    # staged rows may run a different compiled kernel (alignment): same
+    # result to rounding
+    assert O.rel_l2(got[:, :2 * L], w) <= 1e-6
+    assert np.all(np.isnan(got[:, 2 * L:]))
+    # in place on host memory
+    y = x.copy()
+    if op == "conv":
+        f.conv_batch(y, y, K)
+    elif op == "forward":
+        f.forward_batch(y, y)
+    else:
+        f.inverse_batch(y, y)
+    assert O.rel_l2(y[:, :2 * L], w) <= 1e-6
