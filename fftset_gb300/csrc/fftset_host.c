@@ -342,6 +342,7 @@ static int fs_build_resident(struct fs_impl *fs, struct fftset_fft *f)
 		    fgk_plan_resident(&f->vp[v], L, modulation, fs->max_smem, rad, n))
 			return FFTSET_E_UNSUPPORTED;
 		f->vops[v] = ops;
+		f->vtma[v] = tma;
 		vtw[v] = fgk_plan_twiddles(&f->vp[v], NULL);
 	}
 	f->nvar = nvar;
@@ -488,6 +489,22 @@ int fs_is_device_ptr(const void *ptr)
 	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+/* Pinned (page-locked, registered) host memory: kernels reach it directly
+ * over the host link; *dev receives the address kernels use. Pageable host
+ * memory and device memory return 0. */
+static int fs_pinned_host(const void *ptr, const void **dev)
+{
+	struct cudaPointerAttributes a;
+	if (ptr == NULL || cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	if (a.type != cudaMemoryTypeHost || a.devicePointer == NULL)
+		return 0;
+	*dev = a.devicePointer;
+	return 1;
+}
+
 int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 {
 	cudaError_t e;
@@ -524,19 +541,25 @@ int fs_check_flag(struct fs_impl *fs)
  * kernel otherwise. */
 #define FS_STATIC_MIN_COUNT 64
 
-static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *out, const float *in,
-                             const float *kern, unsigned count, size_t in_stride, size_t out_stride,
-                             cudaStream_t stream)
+/* no_bulk: the buffers live in host memory, which this build does not read
+ * with bulk copies (TMA): variants with bulk-copy input are skipped */
+static int fs_launch_variant_ex(const struct fftset_fft *f, int v, int op, float *out, const float *in,
+                                const float *kern, unsigned count, size_t in_stride, size_t out_stride,
+                                cudaStream_t stream, int no_bulk)
 {
 	struct fs_impl *fs = f->fs;
 	if (v >= 0 && v < f->nvar) {
-		int rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, stream,
-		                           fs->num_sms, fs->dev_flag);
+		int rc = -1;
+		if (!(no_bulk && f->vtma[v]))
+			rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, stream,
+			                       fs->num_sms, fs->dev_flag);
 		if (rc >= 0)
 			return rc;
-		/* the variant cannot take these buffers (alignment): any other
-		 * compiled variant that can, else the generic kernel */
+		/* the variant cannot take these buffers (alignment, host memory):
+		 * any other compiled variant that can, else the generic kernel */
 		for (v = 0; v < f->nvar; v++) {
+			if (no_bulk && f->vtma[v])
+				continue;
 			rc = fgk_launch_static(&f->vp[v], v, op, out, in, kern, count, in_stride, out_stride, stream,
 			                       fs->num_sms, fs->dev_flag);
 			if (rc >= 0)
@@ -544,6 +567,13 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 		}
 	}
 	return fgk_launch_resident(&f->rp, op, out, in, kern, count, in_stride, out_stride, stream);
+}
+
+static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *out, const float *in,
+                             const float *kern, unsigned count, size_t in_stride, size_t out_stride,
+                             cudaStream_t stream)
+{
+	return fs_launch_variant_ex(f, v, op, out, in, kern, count, in_stride, out_stride, stream, 0);
 }
 
 int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
@@ -690,7 +720,26 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		return FFTSET_OK;
 	}
 
-	/* host buffers: stage through device memory */
+	/* pinned host buffers (and device ones): resident kernels read and write
+	 * them in place over the host link, no staging copies */
+	if (!f->fourstep) {
+		const void *vin = in, *vout = out, *vkern = kern;
+		const int hin = fs_pinned_host(in, &vin), hout = fs_pinned_host(out, &vout);
+		const int hk = kern != NULL && fs_pinned_host(kern, &vkern);
+		if ((hin || fs_is_device_ptr(in)) && (hout || fs_is_device_ptr(out)) &&
+		    (kern == NULL || hk || fs_is_device_ptr(kern))) {
+			const int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
+			rc = fs_launch_variant_ex(f, v, op, (float *)vout, (const float *)vin, (const float *)vkern, count,
+			                          in_stride, out_stride, fs->stream, 1);
+			if (rc)
+				return rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
+			if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) != 0)
+				return rc;
+			return fs_check_flag(fs);
+		}
+	}
+
+	/* pageable host buffers: stage through device memory */
 	pthread_mutex_lock(&fs->lock);
 	staged = 1;
 	if (!f->fourstep && count > 1 && count * nf * sizeof(float) >= 2 * FS_CHUNK_BYTES &&

@@ -29,6 +29,7 @@ struct fftset_fft {
 	int                             nvar;  /* compile-time kernel variants for this size */
 	fgk_plan                        vp[FS_MAX_VAR]; /* their plans (chain of the variant) */
 	uint32_t                        vops[FS_MAX_VAR]; /* ops each variant implements (1 << op) */
+	uint32_t                        vtma[FS_MAX_VAR]; /* 1: the variant reads its input with bulk copies */
 	int                             sel[FGK_OP_COUNT]; /* chosen variant per op, -1 = generic */
 	int                             fourstep; /* 1: sizes beyond shared memory, two HBM passes */
 	fgk_plan4                       p4;    /* four-step plan (when dmem4 != NULL) */

@@ -461,3 +461,35 @@ def test_host_buffers_chunk_pipeline(gpu_set, mod, L, op):
     else:
         f.inverse_batch(y, y)
     assert O.rel_l2(y[:, :2 * L], w) <= 1e-6
+
+
+@pytest.mark.parametrize("mod,L,op", [(1, 1536, "conv"), (0, 1024, "forward"), (1, 4096, "inverse"),
+                                      (1, 4096, "conv"), (0, 96, "forward")])
+def test_pinned_host_buffers_in_place_access(gpu_set, mod, L, op):
+    """Pinned host buffers are read and written by the kernels directly (no
+    staging): results equal the device-buffer call's to rounding, the memory
+    between padded rows is untouched, in place works."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    B, pad = 300, 6
+    rng = np.random.default_rng(L + 11)
+    x = torch.from_numpy(rng.standard_normal((B, 2 * L + pad)).astype(np.float32)).pin_memory()
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    K = torch.from_numpy(np.empty(2 * L, np.float32)).pin_memory()
+    f.conv_get_kernel(K, torch.from_numpy(h).pin_memory())
+    Kd = K.cuda()
+    xd = x.cuda()[:, :2 * L].contiguous()
+    want = torch.empty(B, 2 * L, device="cuda")
+    got = torch.full((B, 2 * L + 2), float("nan")).pin_memory()
+    call = {"conv": lambda o, i, k: f.conv_batch(o, i, k), "forward": lambda o, i, k: f.forward_batch(o, i),
+            "inverse": lambda o, i, k: f.inverse_batch(o, i)}[op]
+    call(want, xd, Kd)
+    call(got, x, K)
+    w = host(want)
+    g = got.numpy()
+    assert O.rel_l2(g[:, :2 * L], w) <= 1e-6
+    assert np.all(np.isnan(g[:, 2 * L:]))
+    y = x.clone().pin_memory()
+    call(y, y, K)
+    assert O.rel_l2(y.numpy()[:, :2 * L], w) <= 1e-6
+    assert np.array_equal(y.numpy()[:, 2 * L:], x.numpy()[:, 2 * L:])
