@@ -138,8 +138,10 @@ void fftset_destroy(struct fftset *fc)
 	cudaStreamSynchronize(fs->stream);
 	for (p = fs->first; p != NULL; p = n) {
 		n = p->next;
+		fsr_free(p->tasks);
 		cudaFree(p->dmem);
 		cudaFree(p->dmem4);
+		cudaFree(p->dmem3);
 		free(p);
 	}
 	for (i = 0; i < FS_PIPE; i++) {
@@ -308,6 +310,127 @@ out:
 	return rc;
 }
 
+/* Three-level tables (fgk_plan3) in their own device allocation. */
+int fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f)
+{
+	fgk_plan3 *p = &f->p3;
+	const unsigned L = f->lfft;
+	const uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
+	enum { NT = 15 };
+	size_t cnt[NT], off[NT + 1], total, i, k, all = 0;
+	float *h = NULL, *w[NT];
+	char *d = NULL;
+	cudaError_t e;
+	int rc = FFTSET_E_NOMEM;
+	uint32_t L12;
+
+	(void)fs;
+	if (f->dmem3)
+		return FFTSET_OK;
+	if (fgk_plan_threestep(p, L, modulation))
+		return FFTSET_E_UNSUPPORTED;
+	L12 = p->L1 * p->L2;
+	p->tshift = 1;
+	while (((uint64_t)1 << (2 * p->tshift)) < L)
+		p->tshift++;
+	p->ushift = 1;
+	while (((uint64_t)1 << (2 * p->ushift)) < L12)
+		p->ushift++;
+	/* tw1 tw2 tw3 thi tlo uhi ulo tq1 tq2 ma mb mc oa ob oc */
+	cnt[0] = fgk_chain_twiddles(&p->c1, NULL);
+	cnt[1] = fgk_chain_twiddles(&p->c2, NULL);
+	cnt[2] = fgk_chain_twiddles(&p->c3, NULL);
+	cnt[3] = (L + (1u << p->tshift) - 1) >> p->tshift;
+	cnt[4] = (size_t)1 << p->tshift;
+	cnt[5] = (L12 + (1u << p->ushift) - 1) >> p->ushift;
+	cnt[6] = (size_t)1 << p->ushift;
+	cnt[7] = p->nq1;
+	cnt[8] = p->nq2;
+	cnt[9] = cnt[12] = p->L1;
+	cnt[10] = cnt[13] = p->L2;
+	cnt[11] = cnt[14] = p->L3;
+	total = fs_align(sizeof(fgk_plan3));
+	for (i = 0; i < NT; i++) {
+		off[i] = total;
+		total += fs_align((cnt[i] ? cnt[i] : 1) * 2 * sizeof(float));
+		all += cnt[i] ? cnt[i] : 1;
+	}
+	h = (float *)malloc(sizeof(float) * 2 * all);
+	if (!h)
+		goto out;
+	w[0] = h;
+	for (i = 1; i < NT; i++)
+		w[i] = w[i - 1] + 2 * (cnt[i - 1] ? cnt[i - 1] : 1);
+	fgk_chain_twiddles(&p->c1, w[0]);
+	fgk_chain_twiddles(&p->c2, w[1]);
+	fgk_chain_twiddles(&p->c3, w[2]);
+	{
+		/* table i, entry k: e^{-j 2 pi num(k) / den} (FP64, rounded once) */
+		const double twopi = 2.0 * M_PI;
+		for (k = 0; k < cnt[3]; k++) {
+			double a = -twopi * (double)(k << p->tshift) / (double)L;
+			w[3][2 * k] = (float)cos(a), w[3][2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < cnt[4]; k++) {
+			double a = -twopi * (double)k / (double)L;
+			w[4][2 * k] = (float)cos(a), w[4][2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < cnt[5]; k++) {
+			double a = -twopi * (double)(k << p->ushift) / (double)L12;
+			w[5][2 * k] = (float)cos(a), w[5][2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < cnt[6]; k++) {
+			double a = -twopi * (double)k / (double)L12;
+			w[6][2 * k] = (float)cos(a), w[6][2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < cnt[7]; k++) {
+			double a = -twopi * (double)k / (double)p->nq1;
+			w[7][2 * k] = (float)cos(a), w[7][2 * k + 1] = (float)sin(a);
+		}
+		for (k = 0; k < cnt[8]; k++) {
+			double a = -twopi * (double)k / (double)p->nq2;
+			w[8][2 * k] = (float)cos(a), w[8][2 * k + 1] = (float)sin(a);
+		}
+		/* modulation: in e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2 L1 L2)}, e^{-j pi n3/(2L)};
+		 * out e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2 L3)}, e^{-j pi k3/(2 L3)} */
+		{
+			const double den[6] = {2.0 * p->L1, 2.0 * L12, 2.0 * L, 2.0 * L, 2.0 * p->L2 * p->L3, 2.0 * p->L3};
+			for (i = 0; i < 6; i++)
+				for (k = 0; k < cnt[9 + i]; k++) {
+					double a = -M_PI * (double)k / den[i];
+					w[9 + i][2 * k] = (float)cos(a), w[9 + i][2 * k + 1] = (float)sin(a);
+				}
+		}
+	}
+	if ((e = cudaMalloc((void **)&d, total)) != cudaSuccess) {
+		cudaGetLastError();
+		goto out;
+	}
+	{
+		const void **dst[NT] = {&p->tw1, &p->tw2, &p->tw3, &p->thi, &p->tlo, &p->uhi, &p->ulo, &p->tq1, &p->tq2,
+		                        &p->ma,  &p->mb,  &p->mc,  &p->oa,  &p->ob,  &p->oc};
+		for (i = 0; i < NT; i++) {
+			*dst[i] = d + off[i];
+			if (cnt[i] &&
+			    (e = cudaMemcpy(d + off[i], w[i], cnt[i] * 2 * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+				goto cuda_fail;
+		}
+	}
+	p->dev = (const fgk_plan3 *)d;
+	if ((e = cudaMemcpy(d, p, sizeof(fgk_plan3), cudaMemcpyHostToDevice)) != cudaSuccess)
+		goto cuda_fail;
+	f->dmem3 = d;
+	rc = FFTSET_OK;
+	goto out;
+cuda_fail:
+	fs_cuda(fs, e);
+	cudaFree(d);
+	rc = FFTSET_E_CUDA;
+out:
+	free(h);
+	return rc;
+}
+
 /* Build the device tables of a plan: the generic resident plan (chain from
  * the GPU planner) plus one twiddle table per compile-time variant (each
  * variant has its own chain); modulation factors and the kernel-layout index
@@ -434,10 +557,15 @@ const struct fftset_fft *fftset_create_fft(struct fftset *fc, const struct fftse
                                            unsigned complex_bins)
 {
 	struct fs_impl *fs = fs_of(fc);
-	struct fftset_fft *p, **ipos;
-	int rc;
 	if (fs == NULL)
 		return NULL;
+	return fs_create_plan(fs, modulation, complex_bins);
+}
+
+struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modulation *modulation, unsigned complex_bins)
+{
+	struct fftset_fft *p, **ipos;
+	int rc;
 	if (modulation != FFTSET_MODULATION_COMPLEX && modulation != FFTSET_MODULATION_FREQ_OFFSET_REAL) {
 		fs_latch(fs, FFTSET_E_INVALID, 0);
 		return NULL;
@@ -579,6 +707,12 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
                      unsigned count, size_t in_stride, size_t out_stride)
 {
+	if (f->fourstep && (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE)) {
+		/* tile tasks (fgk_tasks.cu): two- or three-level split */
+		const int rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, f->fs->stream);
+		if (rc != -FFTSET_E_UNSUPPORTED)
+			return rc;
+	}
 	if (f->fourstep) {
 		/* two passes through a work buffer of 2L floats per transform (the
 		 * library's own scratch: work_buf of the reference API may be host

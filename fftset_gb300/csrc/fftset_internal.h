@@ -35,6 +35,12 @@ struct fftset_fft {
 	fgk_plan4                       p4;    /* four-step plan (when dmem4 != NULL) */
 	void                           *dmem4; /* its device tables */
 	const int32_t                  *kidx4; /* kernel-layout table in dmem4 */
+	fgk_plan3                       p3;    /* three-level plan (when dmem3 != NULL) */
+	void                           *dmem3; /* its device tables */
+	struct fftset_ragged           *tasks; /* cached task list of the plain calls (fftset_ragged.c) */
+	unsigned                        tasks_count;
+	size_t                          tasks_in_stride, tasks_out_stride;
+	int                             tasks_op;
 	void                           *dmem;  /* one device block for all tables */
 };
 
@@ -69,6 +75,17 @@ int  fs_is_device_ptr(const void *ptr);
 int  fs_check_flag(struct fs_impl *fs);
 /* four-step tables for a plan (built on demand for resident-size plans too) */
 int  fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f);
+/* three-level tables for a plan (sizes beyond 65536 bins), on demand */
+int  fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f);
+/* find-or-create a plan (fftset_create_fft without the public wrapper) */
+struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modulation *modulation, unsigned bins);
+/* forward / inverse of `count` device blocks of a four-step plan as one task
+ * launch (fftset_ragged.c); returns 0, a negative FFTSET_E_* code or a
+ * positive cudaError_t; FFTSET_E_UNSUPPORTED when the size has no tile split */
+int  fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
+                    unsigned count, cudaStream_t stream);
+struct fftset_ragged;
+void fsr_free(struct fftset_ragged *rb);
 struct fs_impl *fs_impl_of(struct fftset *fc);
 /* grows staging slot `slot` to at least `bytes` (cudaMalloc) */
 int  fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);

@@ -1,21 +1,22 @@
-/* Ragged batches: transforms of many different sizes in one submission.
+/* Ragged batches: transforms of many different sizes in one submission, and
+ * the task lists of the plain calls of sizes beyond the shared-memory limit.
  *
- * fftset_ragged_create plans every distinct size through the fftset's own
- * plan cache (fftset_create_fft, so all sizes share the fftset's twiddle
- * tables) and builds the task list of one persistent launch
- * (fgk_tasks.cu), every task a tile of at most fgk_tasks_points() points:
+ * fsr_create plans every distinct size through the fftset's own plan cache
+ * (so all sizes share the fftset's twiddle tables) and builds the task list
+ * of one persistent launch (fgk_tasks.cu), every task a tile of at most
+ * fgk_tasks_points() points:
  *   - items up to fgk_tasks_points() bins: SMALL tasks of same-size items;
- *   - larger items: their four-step split L = L1 L2, COLS tiles (columns
- *     into the item's scratch) then ROWS tiles (rows into the output). The
- *     ROWS tiles of item i are listed after the COLS tiles of item i + D,
- *     D chosen so that two full grids of tasks separate them, so ROWS tiles
- *     rarely wait. Big items need a split with both factors <= 256 (every
- *     size up to 65536 bins has one); larger sizes are refused
- *     (FFTSET_E_UNSUPPORTED) and run through the batched calls instead.
- * Big items come first (largest first), then the SMALL tasks (largest
- * first), which balances the tail. fftset_ragged_execute records the launch
- * into a CUDA graph on first use (and when the base pointers change) and
- * replays the graph afterwards. */
+ *   - items up to 65536 bins: their four-step split L = L1 L2 (both <= 256),
+ *     COLS tiles (columns into the item's scratch) then ROWS tiles (rows
+ *     into the output). The ROWS tiles of item i are listed after the COLS
+ *     tiles of item i + D, D chosen so that two full grids of tasks separate
+ *     them, so ROWS tiles rarely wait;
+ *   - larger items: their three-level split L = L1 L2 L3 (each <= 256),
+ *     pass A, B and C tiles through two scratch areas, each pass after the
+ *     previous one of the same item.
+ * Items run largest first, which balances the tail. fftset_ragged_execute
+ * records the launch into a CUDA graph on first use (and when the base
+ * pointers change) and replays the graph afterwards. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -38,7 +39,8 @@ struct fftset_ragged {
 	fgk_rg_item    *items_dev;
 	fgk_big        *bigs_dev;
 	uint32_t        nbig;
-	uint32_t        nbig_items; /* items run as four-step tiles */
+	fgk_huge       *huges_dev;
+	uint32_t        nhuge;
 	int            *counters_dev;
 	float          *scratch;
 	/* graph */
@@ -93,7 +95,7 @@ static uint32_t fsr_lanes_log2(uint32_t lp, uint32_t count)
 	return ls;
 }
 
-void fftset_ragged_destroy(struct fftset_ragged *rb)
+void fsr_free(struct fftset_ragged *rb)
 {
 	if (!rb)
 		return;
@@ -107,23 +109,29 @@ void fftset_ragged_destroy(struct fftset_ragged *rb)
 	cudaFree(rb->plans_dev);
 	cudaFree(rb->items_dev);
 	cudaFree(rb->bigs_dev);
+	cudaFree(rb->huges_dev);
 	cudaFree(rb->counters_dev);
 	cudaFree(rb->scratch);
 	free(rb);
 }
 
-struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftset_modulation *modulation, int op,
-                                           unsigned n, const unsigned *bins, const size_t *in_offsets,
-                                           const size_t *out_offsets)
+void fftset_ragged_destroy(struct fftset_ragged *rb)
 {
-	struct fs_impl *fs = fs_impl_of(fc);
+	fsr_free(rb);
+}
+
+static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_modulation *modulation, int op,
+                                        unsigned n, const unsigned *bins, const size_t *in_offsets,
+                                        const size_t *out_offsets)
+{
 	struct fftset_ragged *rb = NULL;
 	struct fsr_sort *order = NULL;
 	fgk_plan *plans = NULL;
 	fgk_rg_item *items = NULL;
 	fgk_big *bigs = NULL;
+	fgk_huge *huges = NULL;
 	fgk_task *tasks = NULL;
-	unsigned i, j, nplans = 0, nitems = 0, nbig = 0, ntasks = 0, cap_tasks = 0;
+	unsigned i, j, nplans = 0, nitems = 0, nbig = 0, nhuge = 0, ntasks = 0, cap_tasks = 0;
 	size_t scratch_f2 = 0;
 	uint64_t total_cols = 0;
 	cudaError_t e;
@@ -145,7 +153,8 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	plans = (fgk_plan *)calloc(n, sizeof(*plans));
 	items = (fgk_rg_item *)calloc(n, sizeof(*items));
 	bigs = (fgk_big *)calloc(n, sizeof(*bigs));
-	if (!rb || !order || !plans || !items || !bigs)
+	huges = (fgk_huge *)calloc(n, sizeof(*huges));
+	if (!rb || !order || !plans || !items || !bigs || !huges)
 		goto fail;
 	rb->fs = fs;
 	rb->op = op;
@@ -162,7 +171,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	/* plans, items and big items; SMALL tasks are counted here, listed below */
 	for (i = 0; i < n; i = j) {
 		const unsigned L = order[i].bins;
-		struct fftset_fft *f = (struct fftset_fft *)fftset_create_fft(fc, modulation, L);
+		struct fftset_fft *f = fs_create_plan(fs, modulation, L);
 		for (j = i; j < n && order[j].bins == L; j++)
 			;
 		if (!f) {
@@ -179,6 +188,28 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 			plans[nplans].threads = tg; /* reused below: threads per item */
 			plans[nplans].per_cta = G;  /* and items per task */
 			nplans++;
+		} else if (L > 65536) {
+			/* three-level: pass A, B, C tiles, two scratch areas per item */
+			uint32_t k;
+			const fgk_plan3 *p3;
+			if ((rc = fs_ensure_threestep(fs, f)) != 0)
+				goto fail;
+			p3 = &f->p3;
+			for (k = i; k < j; k++) {
+				fgk_huge *h = &huges[nhuge++];
+				const size_t span = ((size_t)L + 15) & ~(size_t)15;
+				h->p3 = p3->dev;
+				h->in_off = in_offsets[order[k].idx];
+				h->out_off = out_offsets[order[k].idx];
+				h->sa = scratch_f2;
+				h->sb = scratch_f2 + span;
+				scratch_f2 += 2 * span;
+				h->na = (p3->L2 * p3->L3 + 15) / 16;
+				h->nb3 = (p3->L3 + 3) / 4;
+				h->nb = (p3->L1 + 3) / 4 * h->nb3;
+				h->nc1 = (p3->L1 + 15) / 16;
+				cap_tasks += h->na + h->nb + h->nc1 * p3->L2;
+			}
 		} else {
 			uint32_t L1, L2, k;
 			if ((rc = fs_ensure_fourstep(fs, f)) != 0)
@@ -210,6 +241,17 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	tasks = (fgk_task *)malloc(sizeof(*tasks) * (cap_tasks ? cap_tasks : 1));
 	if (!tasks)
 		goto fail;
+	/* three-level items: all A tiles, all B tiles, all C tiles */
+	for (i = 0; i < nhuge; i++) {
+		const struct fftset_fft *f = fs_create_plan(fs, modulation, order[i].bins);
+		uint32_t t;
+		for (t = 0; t < huges[i].na; t++)
+			tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, t, 0};
+		for (t = 0; t < huges[i].nb; t++)
+			tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, t, 0};
+		for (t = 0; t < huges[i].nc1 * f->p3.L2; t++)
+			tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i, t, 0};
+	}
 	/* big items: COLS of item b, ROWS of item b - D */
 	if (nbig) {
 		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms);
@@ -227,7 +269,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	/* small items, largest first */
 	{
 		uint32_t pi = 0;
-		for (i = nbig; i < n; i = j) {
+		for (i = nhuge + nbig; i < n; i = j) {
 			const unsigned L = order[i].bins;
 			uint32_t G, tg;
 			for (j = i; j < n && order[j].bins == L; j++)
@@ -250,12 +292,14 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	}
 	rb->ntasks = ntasks;
 	rb->nbig = nbig;
-	rb->nbig_items = nbig;
+	rb->nhuge = nhuge;
 	if ((e = cudaMalloc((void **)&rb->tasks_dev, sizeof(fgk_task) * (ntasks ? ntasks : 1))) != cudaSuccess ||
 	    (e = cudaMalloc((void **)&rb->plans_dev, sizeof(fgk_plan) * (nplans ? nplans : 1))) != cudaSuccess ||
 	    (e = cudaMalloc((void **)&rb->items_dev, sizeof(fgk_rg_item) * (nitems ? nitems : 1))) != cudaSuccess ||
 	    (e = cudaMalloc((void **)&rb->bigs_dev, sizeof(fgk_big) * (nbig ? nbig : 1))) != cudaSuccess ||
-	    (e = cudaMalloc((void **)&rb->counters_dev, sizeof(int) * (1 + (size_t)nbig))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->huges_dev, sizeof(fgk_huge) * (nhuge ? nhuge : 1))) != cudaSuccess ||
+	    (e = cudaMalloc((void **)&rb->counters_dev, sizeof(int) * (1 + (size_t)nbig + 2 * (size_t)nhuge))) !=
+	        cudaSuccess ||
 	    (scratch_f2 && (e = cudaMalloc((void **)&rb->scratch, scratch_f2 * 2 * sizeof(float))) != cudaSuccess))
 		goto cuda_fail;
 	if ((e = cudaMemcpy(rb->tasks_dev, tasks, sizeof(fgk_task) * ntasks, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -263,7 +307,9 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	                   cudaSuccess) ||
 	    (nitems && (e = cudaMemcpy(rb->items_dev, items, sizeof(fgk_rg_item) * nitems, cudaMemcpyHostToDevice)) !=
 	                   cudaSuccess) ||
-	    (nbig && (e = cudaMemcpy(rb->bigs_dev, bigs, sizeof(fgk_big) * nbig, cudaMemcpyHostToDevice)) != cudaSuccess))
+	    (nbig && (e = cudaMemcpy(rb->bigs_dev, bigs, sizeof(fgk_big) * nbig, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+	    (nhuge &&
+	     (e = cudaMemcpy(rb->huges_dev, huges, sizeof(fgk_huge) * nhuge, cudaMemcpyHostToDevice)) != cudaSuccess))
 		goto cuda_fail;
 	if ((e = cudaStreamCreateWithFlags(&rb->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
 		goto cuda_fail;
@@ -271,6 +317,7 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 	free(plans);
 	free(items);
 	free(bigs);
+	free(huges);
 	free(tasks);
 	return rb;
 cuda_fail:
@@ -282,9 +329,20 @@ fail:
 	free(plans);
 	free(items);
 	free(bigs);
+	free(huges);
 	free(tasks);
-	fftset_ragged_destroy(rb);
+	fsr_free(rb);
 	return NULL;
+}
+
+struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftset_modulation *modulation, int op,
+                                           unsigned n, const unsigned *bins, const size_t *in_offsets,
+                                           const size_t *out_offsets)
+{
+	struct fs_impl *fs = fs_impl_of(fc);
+	if (!fs)
+		return NULL;
+	return fsr_create(fs, modulation, op, n, bins, in_offsets, out_offsets);
 }
 
 /* the launch sequence, on `s` */
@@ -292,8 +350,8 @@ static int fsr_record(struct fftset_ragged *rb, float *out, const float *in, cud
 {
 	struct fs_impl *fs = rb->fs;
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
-	                        rb->counters_dev, rb->scratch, rb->op, rb->modulation, in, out, fs->num_sms, fs->dev_flag,
-	                        s);
+	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, rb->op, rb->modulation, in, out,
+	                        fs->num_sms, fs->dev_flag, s);
 }
 
 int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)
@@ -367,4 +425,56 @@ double fftset_ragged_bytes(const struct fftset_ragged *rb)
 unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb)
 {
 	return rb ? rb->n : 0; /* every item runs in the one persistent launch */
+}
+
+/* The plain calls (forward / inverse, device buffers) of a plan beyond the
+ * shared-memory limit: `count` items of its size at b * stride, one task
+ * launch on `stream`. The task list is kept on the plan for the last (count,
+ * strides, op) seen. */
+int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
+                   unsigned count, cudaStream_t stream)
+{
+	struct fs_impl *fs = f->fs;
+	const size_t nf = 2 * (size_t)f->lfft;
+	if (count == 0)
+		return 0;
+	if (count == 1)
+		in_stride = out_stride = nf;
+	if (!f->tasks || f->tasks_count != count || f->tasks_in_stride != in_stride ||
+	    f->tasks_out_stride != out_stride || f->tasks_op != op) {
+		unsigned *bins = (unsigned *)malloc(sizeof(unsigned) * count);
+		size_t *io = (size_t *)malloc(sizeof(size_t) * count), *oo = (size_t *)malloc(sizeof(size_t) * count);
+		unsigned b;
+		int err0 = fs->err;
+		if (!bins || !io || !oo) {
+			free(bins);
+			free(io);
+			free(oo);
+			return -FFTSET_E_NOMEM;
+		}
+		for (b = 0; b < count; b++) {
+			bins[b] = f->lfft;
+			io[b] = b * in_stride;
+			oo[b] = b * out_stride;
+		}
+		fsr_free(f->tasks);
+		f->tasks = fsr_create(fs, f->modulator, op, count, bins, io, oo);
+		free(bins);
+		free(io);
+		free(oo);
+		if (!f->tasks) {
+			/* no tile split for this size: the caller falls back; leave the
+			 * latched error as it was */
+			if (!err0 && fs->err == FFTSET_E_UNSUPPORTED) {
+				fs->err = 0;
+				fs->cuda_err = 0;
+			}
+			return -FFTSET_E_UNSUPPORTED;
+		}
+		f->tasks_count = count;
+		f->tasks_in_stride = in_stride;
+		f->tasks_out_stride = out_stride;
+		f->tasks_op = op;
+	}
+	return fsr_record(f->tasks, out, in, stream);
 }

@@ -79,6 +79,27 @@ typedef struct fgk_plan4 {
 	const struct fgk_plan4 *dev;
 } fgk_plan4;
 
+/* Plan of a three-level transform L = L1 L2 L3 (each <= 256, L1 >= 16) run
+ * as tile tasks (fgk_tasks.cu): n = (n1 L2 + n2) L3 + n3,
+ * k = k1 + L1 (k2 + L2 k3).
+ *   pass A: DFT_L1 over n1, times w_{L1 L2}^{n2 k1}, into A[k1][n2 L3 + n3];
+ *   pass B: DFT_L2 over n2, times w_L^{n3 (k1 + L1 k2)}, into
+ *           B[(k2 L3 + n3) L1 + k1];
+ *   pass C: DFT_L3 over n3 into X[k1 + L1 k2 + L1 L2 k3]. */
+typedef struct fgk_plan3 {
+	uint32_t    L1, L2, L3, modulation;
+	uint32_t    tshift;          /* w_L^m = thi[m >> tshift] tlo[m & (2^tshift - 1)] */
+	uint32_t    ushift;          /* w_{L1 L2}^m = uhi[m >> ushift] ulo[m & (2^ushift - 1)] */
+	uint32_t    nq1, nq2;        /* R1 L2 and R2 L3, R1 / R2 the last radices of c1 / c2 */
+	fgk_chain   c1, c2, c3;
+	const void *tw1, *tw2, *tw3; /* chain twiddles */
+	const void *thi, *tlo, *uhi, *ulo;
+	const void *tq1, *tq2;       /* w_{R1 L2}^m, w_{R2 L3}^m */
+	const void *ma, *mb, *mc;    /* e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2 L1 L2)}, e^{-j pi n3/(2L)} */
+	const void *oa, *ob, *oc;    /* e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2 L3)}, e^{-j pi k3/(2 L3)} */
+	const struct fgk_plan3 *dev;
+} fgk_plan3;
+
 /* Ragged batches: item offsets in floats from the batch's base pointers. */
 typedef struct fgk_rg_item {
 	uint64_t in_off, out_off;
@@ -92,7 +113,14 @@ typedef struct fgk_rg_item {
  *   ROWS   lanes of rows of that scratch (DFTs of length L2 into the
  *          output); they start once every COLS tile of the item is done. */
 
-enum fgk_task_kind { FGK_TASK_SMALL = 0, FGK_TASK_COLS = 1, FGK_TASK_ROWS = 2 };
+enum fgk_task_kind {
+	FGK_TASK_SMALL = 0,
+	FGK_TASK_COLS = 1,
+	FGK_TASK_ROWS = 2,
+	FGK_TASK_PA = 3, /* three-level passes (fgk_plan3) */
+	FGK_TASK_PB = 4,
+	FGK_TASK_PC = 5
+};
 
 typedef struct fgk_task {
 	uint32_t kind;
@@ -100,6 +128,16 @@ typedef struct fgk_task {
 	uint32_t a;    /* SMALL: first item; COLS/ROWS: tile index */
 	uint32_t b;    /* SMALL: items | threads per item << 16 */
 } fgk_task;
+
+/* A three-level item: passes A, B, C through two scratch areas; B tiles
+ * wait for every A tile of the item, C tiles for every B tile. */
+typedef struct fgk_huge {
+	const struct fgk_plan3 *p3;             /* device copy of the item's plan */
+	uint64_t                in_off, out_off; /* floats from the batch's base pointers */
+	uint64_t                sa, sb;          /* float2 offsets of its A and B scratch */
+	uint32_t                na, nb;          /* A tiles, B tiles */
+	uint32_t                nb3, nc1;        /* B tiles per k1 group (ceil(L3/4)), C tiles per k2 (ceil(L1/16)) */
+} fgk_huge;
 
 typedef struct fgk_big {
 	const struct fgk_plan4 *p4;            /* device copy of the item's four-step plan */
@@ -120,6 +158,9 @@ size_t fgk_plan_twiddles(fgk_plan *p, void *tw_host_float2);
 /* Four-step planning: fills sizes, lanes, threads and chains (not the
  * pointers). Returns -1 when L has no two-factor split the kernels take. */
 int    fgk_plan_fourstep(fgk_plan4 *p, uint32_t L, uint32_t modulation, uint32_t max_smem_bytes);
+/* Three-level split of L (each factor <= 256, L1 >= 16, most balanced);
+ * fills sizes and chains. Returns -1 when L has none. */
+int    fgk_plan_threestep(fgk_plan3 *p, uint32_t L, uint32_t modulation);
 /* twiddles of one chain (the chain's tw_off fields are set) */
 size_t fgk_chain_twiddles(fgk_chain *c, void *tw_host_float2);
 
@@ -133,12 +174,14 @@ uint32_t fgk_max_resident_L(void);
 int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
                         const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
                         size_t out_stride, size_t work_stride, void *stream);
-/* the task launch: counters_dev holds 1 + nbig ints (claim counter, then the
- * finished COLS tiles of each big item) and is reset by the launcher;
+/* the task launch: counters_dev holds 1 + nbig + 2 nhuge ints (claim counter,
+ * the finished COLS tiles of each big item, the finished A and B tiles of
+ * each three-level item) and is reset by the launcher;
  * scratch_dev holds the big items' L1 x L2 intermediates; err_flag is set
  * when a bounded wait gives up */
 int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
-                        const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig, int *counters_dev,
+                        const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
+                        const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev,
                         float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
                         int num_sms, int *err_flag, void *stream);
 int    fgk_tasks_grid(int num_sms);

@@ -324,3 +324,51 @@ int fgk_plan_fourstep(fgk_plan4 *p, uint32_t L, uint32_t modulation, uint32_t ma
 		return -1;
 	return 0;
 }
+
+/* Three-level split: L1 in [16, 256], L2, L3 <= 256, L1 L2 L3 = L, the
+ * smallest largest factor, ties towards L1 a multiple of 16 (whole C tiles). */
+int fgk_plan_threestep(fgk_plan3 *p, uint32_t L, uint32_t modulation)
+{
+	uint32_t a, b, c, L1, L2, best = 0, b1 = 0, b2 = 0, bmul = 0, rad[FGK_MAX_STAGES], n;
+	memset(p, 0, sizeof(*p));
+	if (factor235(L, &a, &b, &c))
+		return -1;
+	for (L1 = 16; L1 <= 256; L1++) {
+		if (L % L1)
+			continue;
+		for (L2 = 2; L2 <= 256; L2++) {
+			uint32_t L3, m;
+			if ((L / L1) % L2)
+				continue;
+			L3 = L / L1 / L2;
+			if (L3 < 2 || L3 > 256)
+				continue;
+			m = L1 > L2 ? L1 : L2;
+			m = m > L3 ? m : L3;
+			if (!best || m < best || (m == best && (L1 % 16 == 0) && !bmul)) {
+				best = m;
+				b1 = L1;
+				b2 = L2;
+				bmul = L1 % 16 == 0;
+			}
+		}
+	}
+	if (!best)
+		return -1;
+	p->L1 = b1;
+	p->L2 = b2;
+	p->L3 = L / b1 / b2;
+	p->modulation = modulation;
+	if (plan_chain_set(p->L1, FGK_ALL_RADICES, rad, &n))
+		return -1;
+	fill_chain(&p->c1, rad, n, p->L1, 256);
+	if (plan_chain_set(p->L2, FGK_ALL_RADICES, rad, &n))
+		return -1;
+	fill_chain(&p->c2, rad, n, p->L2, 256);
+	if (plan_chain_set(p->L3, FGK_ALL_RADICES, rad, &n))
+		return -1;
+	fill_chain(&p->c3, rad, n, p->L3, 256);
+	p->nq1 = p->c1.st[p->c1.nstages - 1].radix * p->L2;
+	p->nq2 = p->c2.st[p->c2.nstages - 1].radix * p->L3;
+	return 0;
+}

@@ -253,6 +253,44 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	}
 }
 
+/* Bounded wait of a whole CTA until *ctr >= need (thread 0 polls with an
+ * acquire load, then a barrier). On timeout the error flag is raised and
+ * false returned: the caller skips its tile. */
+__device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int *failed)
+{
+	if (threadIdx.x == 0) {
+		int f = 0;
+		uint32_t it = 0;
+		for (;;) {
+			int d;
+			asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(d) : "l"(ctr) : "memory");
+			if (d >= need)
+				break;
+			if (++it > TK_SPIN_LIMIT) {
+				f = 1;
+				if (err)
+					atomicExch(err, 1);
+				break;
+			}
+			__nanosleep(256);
+		}
+		__threadfence();
+		*failed = f;
+	}
+	__syncthreads();
+	return !*failed;
+}
+
+/* A tile's scratch stores, then one gpu-scope release of its count */
+__device__ __forceinline__ void tk_signal(int *ctr)
+{
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		__threadfence();
+		atomicAdd(ctr, 1);
+	}
+}
+
 /* ---- SMALL: whole items side by side ---------------------------------- */
 /* n items of one size, tg threads each (group g = threadIdx / tg), each
  * group's first stage reading its item and its last stage writing its
@@ -358,12 +396,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 	};
 	tile_chain<true, Rows>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                       (int)blockDim.x, true, ld, st, [] {});
-	/* the CTA's scratch stores, then one gpu-scope release of the count */
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		__threadfence();
-		atomicAdd(done, 1);
-	}
+	tk_signal(done);
 }
 
 /* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
@@ -381,27 +414,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
 
 	/* every COLS tile of this item, bounded */
-	if (tid == 0) {
-		int f = 0;
-		uint32_t it = 0;
-		for (;;) {
-			int d;
-			asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(d) : "l"(done) : "memory");
-			if (d >= (int)bg.ncols)
-				break;
-			if (++it > TK_SPIN_LIMIT) {
-				f = 1;
-				if (err)
-					atomicExch(err, 1);
-				break;
-			}
-			__nanosleep(256);
-		}
-		__threadfence();
-		*failed = f;
-	}
-	__syncthreads();
-	if (*failed)
+	if (!tk_wait(done, (int)bg.ncols, err, failed))
 		return;
 
 	const float2 *Stile = scratch + bg.scratch_off + (uint64_t)tk.a * ((uint64_t)L2 << ls);
@@ -442,14 +455,152 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 	                        discard);
 }
 
+/* ---- three-level items (fgk_plan3): passes A, B, C ------------------- */
+/* A: 16 adjacent columns c = n2 L3 + n3, DFT_L1 over n1 straight from the
+ * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
+ * A[k1][c] (a warp's 16 lanes write one 128-byte segment). */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
+                                        float2 *scratch, int *done, float2 *smem)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L3 = (int)p->L3;
+	const uint32_t L23 = p->L2 * p->L3, L = (uint32_t)L1 * L23;
+	const int cbase = (int)(tk.a << 4);
+	const float inv3 = 1.0f / (float)L3;
+	const float *x = in_base + hg.in_off;
+	const float2 *x2 = reinterpret_cast<const float2 *>(x);
+	const float2 *ma = (const float2 *)p->ma, *mb = (const float2 *)p->mb, *mc = (const float2 *)p->mc;
+	const float2 *uhi = (const float2 *)p->uhi, *ulo = (const float2 *)p->ulo, *tq = (const float2 *)p->tq1;
+	const uint32_t ush = p->ushift, umask = (1u << ush) - 1;
+	float2 *A = scratch + hg.sa;
+	auto ld = [&](int n1, int lane) {
+		const uint32_t c = (uint32_t)(cbase + lane);
+		if (c >= L23)
+			return make_float2(0.f, 0.f);
+		const uint32_t n = (uint32_t)n1 * L23 + c;
+		if (!inverse) {
+			if (freq) {
+				const int n2 = tk_div((int)c, L3, inv3), n3 = (int)c - n2 * L3;
+				const float2 m = cmul(__ldg(ma + n1), cmul(__ldg(mb + n2), __ldg(mc + n3)));
+				return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), m);
+			}
+			return __ldcs(x2 + n);
+		}
+		if (freq)
+			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
+		return conjf2(__ldcs(x2 + n));
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const uint32_t c = (uint32_t)(cbase + lane);
+		if (c >= L23)
+			return;
+		const int n2 = tk_div((int)c, L3, inv3);
+		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
+		const float2 b = cmul(__ldg(uhi + (m >> ush)), __ldg(ulo + (m & umask)));
+		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : b;
+		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
+	};
+	tile_chain<false, Rows>(&p->c1, (const float2 *)p->tw1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+	tk_signal(done);
+}
+
+/* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
+ * n2 from A (32-byte segments), times w_L^{n3 (k1 + L1 k2)} =
+ * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
+                                        int *done_b, int *err, float2 *smem, int *failed)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const uint32_t L23 = (uint32_t)L2 * L3;
+	const int k1g = (int)(tk.a / hg.nb3);
+	const int k1b = k1g * 4, n3b = (int)(tk.a - (uint32_t)k1g * hg.nb3) * 4;
+	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo, *tq = (const float2 *)p->tq2;
+	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
+	const float2 *A = scratch + hg.sa;
+	float2 *B = scratch + hg.sb;
+	if (!tk_wait(done_a, (int)hg.na, err, failed))
+		return;
+	auto ld = [&](int n2, int lane) {
+		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
+		if (k1 >= L1 || n3 >= L3)
+			return make_float2(0.f, 0.f);
+		return __ldcg(A + (uint32_t)k1 * L23 + (uint32_t)n2 * L3 + n3);
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
+		if (k1 >= L1 || n3 >= L3)
+			return;
+		const uint32_t m = (uint32_t)n3 * ((uint32_t)k1 + (uint32_t)L1 * (uint32_t)j);
+		const float2 b = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
+		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
+	};
+	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+	tk_signal(done_b);
+}
+
+/* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from B (128-byte segments),
+ * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
+                                        const int *done_b, int *err, float2 *smem, int *failed)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const uint32_t L = (uint32_t)L1 * L2 * L3;
+	const int k2 = (int)(tk.a / hg.nc1);
+	const int k1b = (int)(tk.a - (uint32_t)k2 * hg.nc1) * 16;
+	const float2 *B = scratch + hg.sb;
+	float *o = out_base + hg.out_off;
+	float2 *o2 = reinterpret_cast<float2 *>(o);
+	const float2 *oa = (const float2 *)p->oa, *ob = (const float2 *)p->ob, *oc = (const float2 *)p->oc;
+	if (!tk_wait(done_b, (int)hg.nb, err, failed))
+		return;
+	auto ld = [&](int n3, int lane) {
+		const int k1 = k1b + lane;
+		if (k1 >= L1)
+			return make_float2(0.f, 0.f);
+		return __ldcg(B + ((uint32_t)k2 * L3 + n3) * (uint32_t)L1 + k1);
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const int k1 = k1b + lane;
+		if (k1 >= L1)
+			return;
+		const int k3 = j + q * nbf;
+		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * ((uint32_t)k2 + (uint32_t)L2 * k3);
+		if (!inverse) {
+			if (!freq)
+				__stcs(o2 + m, v);
+			else if (m < ((L + 1) >> 1))
+				__stcs(o2 + 2 * m, v);
+			else
+				__stcs(o2 + 2 * (L - 1 - m) + 1, conjf2(v));
+		} else if (freq) {
+			const float2 r = cmul(v, cmul(__ldg(oa + k1), cmul(__ldg(ob + k2), __ldg(oc + k3))));
+			__stcs(o + m, r.x);
+			__stcs(o + L + m, r.y);
+		} else {
+			__stcs(o2 + m, conjf2(v));
+		}
+	};
+	tile_chain<false, Rows>(&p->c3, (const float2 *)p->tw3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+}
+
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the
  * current one starts, so the claim's round trip overlaps the work. One
  * instantiation per (direction, modulation): a batch has one of each. */
 template <bool inverse, bool freq>
 __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
-                const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs, int *counters,
-                float2 *scratch, const float *in_base, float *out_base, int *err)
+                const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
+                const fgk_huge *__restrict__ huges, int *counters, int *hcounters, float2 *scratch,
+                const float *in_base, float *out_base, int *err)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
@@ -473,9 +624,17 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem);
 		else if (tk.kind == FGK_TASK_COLS)
 			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem);
-		else
+		else if (tk.kind == FGK_TASK_ROWS)
 			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, smem,
 			                         &failed);
+		else if (tk.kind == FGK_TASK_PA)
+			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem);
+		else if (tk.kind == FGK_TASK_PB)
+			task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref, hcounters + 2 * tk.ref + 1, err,
+			                       smem, &failed);
+		else
+			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, smem,
+			                       &failed);
 		__syncthreads(); /* buffers are reused by the next task */
 		if (threadIdx.x == 0) {
 			cur = ahead;
@@ -510,8 +669,9 @@ extern "C" int fgk_tasks_grid(int num_sms)
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
-                                int *counters_dev, float *scratch_dev, int op, int modulation, const float *in_base,
-                                float *out_base, int num_sms, int *err_flag, void *stream)
+                                const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev, float *scratch_dev,
+                                int op, int modulation, const float *in_base, float *out_base, int num_sms,
+                                int *err_flag, void *stream)
 {
 	using namespace fgk;
 	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
@@ -524,12 +684,14 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	if ((e = cudaFuncSetAttribute((const void *)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
 	    cudaSuccess)
 		return (int)e;
-	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig), (cudaStream_t)stream)) != cudaSuccess)
+	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig + 2 * (size_t)nhuge),
+	                         (cudaStream_t)stream)) != cudaSuccess)
 		return (int)e;
 	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms);
 	if (grid > ntasks)
 		grid = ntasks;
-	k<<<grid, TK_THREADS, smem, (cudaStream_t)stream>>>(tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, counters_dev,
+	k<<<grid, TK_THREADS, smem, (cudaStream_t)stream>>>(tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, huges_dev,
+	                                                    counters_dev, counters_dev + 1 + nbig,
 	                                                    reinterpret_cast<float2 *>(scratch_dev), in_base, out_base,
 	                                                    err_flag);
 	return (int)cudaGetLastError();

@@ -163,8 +163,9 @@ int fftset_fft_autotune(const struct fftset_fft *fft, int op, unsigned count, fl
  * from input_base + in_offsets[i] and written to output_base + out_offsets[i]
  * (offsets in floats, even; device buffers). All sizes share the fftset's
  * plans and twiddles. Every item runs in one persistent launch of tile tasks
- * (items up to 4096 bins whole; larger ones as the column and row tiles of
- * their four-step split, through a scratch buffer that L2 serves), captured
+ * (items up to 4096 bins whole; up to 65536 bins as the column and row tiles
+ * of their four-step split, through a scratch buffer that L2 serves; larger
+ * ones as the three passes of a three-level split), captured
  * in a CUDA graph on the first execute (again when the base pointers change)
  * and replayed. fftset_ragged_execute reports FFTSET_E_TIMEOUT if a tile's
  * bounded wait gave up. */

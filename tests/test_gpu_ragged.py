@@ -32,7 +32,8 @@ def layout(sizes, gap=2):
 def test_ragged_forward_inverse(fftset_lib, gpu_set, mod, graph):
     import torch
     sizes = draw_sizes(240, seed=4 + mod)
-    sizes[:3] = [65536, 59049, 60]          # largest, odd four-step, smallest
+    # three-level (beyond 65536), largest two-level, odd two-level, smallest
+    sizes[:4] = [393216, 65536, 59049, 60]
     offs, total = layout(sizes)
     rng = np.random.default_rng(5)
     x = rng.uniform(-1, 1, total).astype(np.float32)
@@ -82,6 +83,4 @@ def test_ragged_rejects_bad_input(fftset_lib, gpu_set):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 7], [0, 200], [0, 200])
     with pytest.raises(fftset_lib.FftsetError):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64], [1], [0])
-    # items beyond 65536 bins have no split with both factors <= 256
-    with pytest.raises(fftset_lib.FftsetError):
-        fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 131072], [0, 128], [0, 128])
+
