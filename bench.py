@@ -531,7 +531,8 @@ def run_gb300(args):
 def profile_case(args):
     """A small fixed case of one workload for ncu captures (no timing, no
     JSON line): `ragged` = the first --items items of the ragged draw, one
-    launch per execute (no graph), executed three times."""
+    launch per execute (no graph), executed three times; `large` = three
+    forward+inverse pairs of the 15,728,640-bin FREQ_OFFSET_REAL transform."""
     import torch
     import fftset_gb300 as fs
     if args.profile == "ragged":
@@ -552,6 +553,20 @@ def profile_case(args):
         torch.cuda.synchronize()
         S.check()
         print(json.dumps({"profile": "ragged", "items": len(sizes), "bytes": rb.bytes}))
+    elif args.profile == "large":
+        L = 15728640
+        S = fs.FftSet()
+        S.set_stream(torch.cuda.current_stream())
+        S.set_blocking(False)
+        f = S.create_fft(fs.FREQ_OFFSET_REAL, L)
+        x = torch.from_numpy(np.random.default_rng(6).standard_normal(2 * L).astype(np.float32)).cuda()
+        X = torch.empty_like(x)
+        for _ in range(3):
+            f.forward(X, x)
+            f.inverse(x, X)
+        torch.cuda.synchronize()
+        S.check()
+        print(json.dumps({"profile": "large", "bins": L}))
 
 
 def main():
@@ -564,7 +579,7 @@ def main():
                     help="only the headline workload (no per-call, ragged, large and adjoint lines)")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin the conv kernel variant (-1 generic) instead of autotuning")
-    ap.add_argument("--profile", choices=["ragged"], default=None,
+    ap.add_argument("--profile", choices=["ragged", "large"], default=None,
                     help="run one small fixed case for an ncu capture instead of the benchmark")
     ap.add_argument("--items", type=int, default=2000, help="items of the --profile ragged case")
     args = ap.parse_args()

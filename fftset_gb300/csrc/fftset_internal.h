@@ -40,7 +40,6 @@ struct fftset_fft {
 	struct fftset_ragged           *tasks; /* cached task list of the plain calls (fftset_ragged.c) */
 	unsigned                        tasks_count;
 	size_t                          tasks_in_stride, tasks_out_stride;
-	int                             tasks_op;
 	void                           *dmem;  /* one device block for all tables */
 };
 

@@ -430,7 +430,7 @@ unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb)
 /* The plain calls (forward / inverse, device buffers) of a plan beyond the
  * shared-memory limit: `count` items of its size at b * stride, one task
  * launch on `stream`. The task list is kept on the plan for the last (count,
- * strides, op) seen. */
+ * strides) seen; the direction is chosen at launch. */
 int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
                    unsigned count, cudaStream_t stream)
 {
@@ -441,7 +441,7 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 	if (count == 1)
 		in_stride = out_stride = nf;
 	if (!f->tasks || f->tasks_count != count || f->tasks_in_stride != in_stride ||
-	    f->tasks_out_stride != out_stride || f->tasks_op != op) {
+	    f->tasks_out_stride != out_stride) {
 		unsigned *bins = (unsigned *)malloc(sizeof(unsigned) * count);
 		size_t *io = (size_t *)malloc(sizeof(size_t) * count), *oo = (size_t *)malloc(sizeof(size_t) * count);
 		unsigned b;
@@ -474,7 +474,7 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 		f->tasks_count = count;
 		f->tasks_in_stride = in_stride;
 		f->tasks_out_stride = out_stride;
-		f->tasks_op = op;
 	}
+	f->tasks->op = op; /* the task list does not depend on the direction */
 	return fsr_record(f->tasks, out, in, stream);
 }
