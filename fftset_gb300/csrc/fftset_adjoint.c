@@ -9,7 +9,8 @@
  *                  the negacyclic (FREQ_OFFSET_REAL) or cyclic (COMPLEX)
  *                  cross-correlation of g_b with h;
  *   grad_taps    = inverse( sum_b G_b conj(X_b) ), the gradient with respect
- *                  to the taps h (fgk_adjoint.cu).
+ *                  to the taps h: batched forward transforms of g and x into
+ *                  scratch, column sums (fgk_adjoint.cu), the plan's inverse.
  * For FREQ_OFFSET_REAL (real data) these are the gradients of a real loss;
  * for COMPLEX they are the adjoint linear maps. */
 #include <stdint.h>
@@ -22,13 +23,10 @@
 #include "fgk.h"
 
 #define FSA_SLOT 4                       /* staging slot of the adjoint's scratch */
-#define FSA_SPEC_CAP ((size_t)256 << 20) /* bytes of spectra per sub-batch (unfused path) */
-#define FSA_CHUNKS 64                    /* partial rows per sub-batch (unfused path) */
+#define FSA_SPEC_CAP ((size_t)256 << 20) /* bytes of spectra per sub-batch */
+#define FSA_CHUNKS 64                    /* partial rows per sub-batch */
 
 /* implemented in fgk_adjoint.cu */
-int fgk_kgrad_fused_shape(const fgk_plan *p, uint32_t *T, uint32_t *G, size_t *smem);
-int fgk_launch_kgrad_fused(const fgk_plan *p, const float *grad_out, size_t g_stride, const float *x,
-                           size_t x_stride, uint32_t count, uint32_t grid, float *partials, void *stream);
 int fgk_launch_kgrad_spec(const float *S, const float *X, size_t stride, uint32_t count, uint32_t L, uint32_t chunk,
                           float *partials, void *stream);
 int fgk_launch_kgrad_reduce(const float *partials, uint32_t P, uint32_t L, int pack, float *out, void *stream);
@@ -45,35 +43,9 @@ static int fsa_rc(struct fs_impl *fs, int rc)
 	return rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
 }
 
-/* grad_taps for a plan whose three transform buffers fit one CTA */
-static int fsa_taps_fused(const struct fftset_fft *f, float *grad_taps, const float *g, size_t g_stride,
-                          const float *x, size_t x_stride, unsigned count, uint32_t G)
-{
-	struct fs_impl *fs = f->fs;
-	const size_t L = f->lfft, nf = 2 * L;
-	uint32_t grid = (uint32_t)((count + G - 1) / G);
-	size_t P, part_floats;
-	float *partials, *S;
-	int rc;
-	if (grid > (uint32_t)fs->num_sms)
-		grid = (uint32_t)fs->num_sms;
-	P = (size_t)grid * G;
-	part_floats = fsa_align(P * nf);
-	if ((rc = fs_stage_reserve(fs, FSA_SLOT, (part_floats + nf) * sizeof(float))) != 0)
-		return -rc;
-	partials = (float *)fs->stage[FSA_SLOT];
-	S = partials + part_floats;
-	if ((rc = fgk_launch_kgrad_fused(&f->rp, g, g_stride, x, x_stride, count, grid, partials, fs->stream)) != 0)
-		return rc;
-	if ((rc = fgk_launch_kgrad_reduce(partials, (uint32_t)P, (uint32_t)L,
-	                                  f->modulator->freq_offset_real ? 1 : 0, S, fs->stream)) != 0)
-		return rc;
-	return fs_launch(f, FGK_OP_INVERSE, grad_taps, S, NULL, 1, 0, 0);
-}
-
-/* grad_taps for any plan: batched forward transforms into scratch, column
- * sums of G conj(X), then the inverse */
-static int fsa_taps_unfused(const struct fftset_fft *f, float *grad_taps, const float *g, size_t g_stride,
+/* grad_taps: batched forward transforms into scratch, column sums of
+ * G conj(X), then the inverse */
+static int fsa_taps(const struct fftset_fft *f, float *grad_taps, const float *g, size_t g_stride,
                             const float *x, size_t x_stride, unsigned count)
 {
 	struct fs_impl *fs = f->fs;
@@ -120,8 +92,6 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 {
 	struct fs_impl *fs;
 	size_t nf;
-	uint32_t T, G;
-	size_t smem;
 	int rc = 0;
 
 	if (fft == NULL)
@@ -164,10 +134,7 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 			goto done;
 	}
 	if (grad_taps) {
-		if (!fft->fourstep && fgk_kgrad_fused_shape(&fft->rp, &T, &G, &smem))
-			rc = fsa_taps_fused(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count, G);
-		else
-			rc = fsa_taps_unfused(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
+		rc = fsa_taps(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
 		if ((rc = fsa_rc(fs, rc)) != 0)
 			goto done;
 	}

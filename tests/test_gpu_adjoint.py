@@ -1,8 +1,7 @@
 """The convolution adjoint (fftset_fft_conv_adjoint_batch) through the C ABI
 and a torch.autograd.Function harness (tests/fftset_autograd.py):
-  - against the FP64 adjoint (oracle.conv_adjoint64) for both modulations and
-    every code path (fused kernel, unfused for sizes whose buffers do not fit,
-    four-step sizes), with ragged strides and in-place-style aliasing rules;
+  - against the FP64 adjoint (oracle.conv_adjoint64) for both modulations at
+    resident, four-step and three-level sizes, with padded strides;
   - against reference gradients built from the reference's own CPU
     convolution with time-reversed kernels (tests/golden/ref_adjoint_vw4.npz);
   - the differentiable batched workload (FREQ_OFFSET_REAL, 4096 bins, batch
@@ -44,9 +43,8 @@ def adjoint(f, g, x, h):
     return host(dx), host(dh)
 
 
-# fused (60 .. 8192), unfused (8748: three buffers fit, threads do not;
-# 16384: buffers do not fit), four-step (32768)
-SIZES = [(1, 60), (1, 96), (1, 243), (1, 1536), (1, 4096), (1, 8192), (1, 8748), (1, 16384), (1, 32768),
+# resident (60 .. 16384), four-step (32768, 131072 three-level)
+SIZES = [(1, 60), (1, 96), (1, 243), (1, 1536), (1, 4096), (1, 8192), (1, 8748), (1, 16384), (1, 32768), (1, 131072),
          (0, 64), (0, 1024), (0, 4096), (0, 11520), (0, 32768)]
 
 
