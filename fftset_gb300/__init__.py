@@ -78,6 +78,7 @@ _decl("fftset_ragged_set_graph", C.c_int, [_vp, C.c_int])
 _decl("fftset_ragged_bytes", C.c_double, [_vp])
 _decl("fftset_ragged_persistent_items", _u, [_vp])
 _decl("fftset_ragged_destroy", None, [_vp])
+_decl("fftset_ragged_autotune", C.c_int, [_vp])
 _decl("fftset_fft_conv_adjoint_batch", C.c_int, [_vp, _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _u])
 
 MODULATION_COMPLEX = _vp.in_dll(_lib, "FFTSET_MODULATION_COMPLEX").value
@@ -341,6 +342,16 @@ class Ragged:
 
     def set_graph(self, enable: bool):
         _lib.fftset_ragged_set_graph(self.h, 1 if enable else 0)
+
+    def autotune(self):
+        """fftset_ragged_autotune: per-size schedules by timing, then a
+        rebuilt task list."""
+        import torch
+        self.owner.set_stream(torch.cuda.current_stream())
+        rc = _lib.fftset_ragged_autotune(self.h)
+        if rc:
+            self.owner.check()
+            raise FftsetError(error_string(rc))
 
     def execute(self, out, inp):
         import torch

@@ -139,6 +139,7 @@ void fftset_destroy(struct fftset *fc)
 	for (p = fs->first; p != NULL; p = n) {
 		n = p->next;
 		fsr_free(p->tasks);
+		cudaFree(p->rg_dmem);
 		cudaFree(p->dmem);
 		cudaFree(p->dmem4);
 		cudaFree(p->dmem3);

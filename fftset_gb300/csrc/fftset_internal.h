@@ -38,6 +38,14 @@ struct fftset_fft {
 	fgk_plan3                       p3;    /* three-level plan (when dmem3 != NULL) */
 	void                           *dmem3; /* its device tables */
 	struct fftset_ragged           *tasks; /* cached task list of the plain calls (fftset_ragged.c) */
+	/* task-kernel schedule picked by fftset_ragged_autotune (rg_tuned):
+	 * whole items run rg_plan's chain (its tables in rg_dmem, NULL for the
+	 * default chain) with rg_tg threads each; two-level items use rg_ls1 /
+	 * rg_ls2 lanes per COLS / ROWS tile */
+	int                             rg_tuned;
+	fgk_plan                        rg_plan;
+	void                           *rg_dmem;
+	uint32_t                        rg_tg, rg_ls1, rg_ls2;
 	unsigned                        tasks_count;
 	size_t                          tasks_in_stride, tasks_out_stride;
 	void                           *dmem;  /* one device block for all tables */

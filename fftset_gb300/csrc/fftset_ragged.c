@@ -50,6 +50,10 @@ struct fftset_ragged {
 	float          *g_out;
 	int             use_graph;
 	double          bytes;
+	/* the creation arguments (a rebuild after autotuning) */
+	const struct fftset_modulation *mod;
+	unsigned       *bins;
+	size_t         *in_offsets, *out_offsets;
 };
 
 struct fsr_sort {
@@ -112,6 +116,9 @@ void fsr_free(struct fftset_ragged *rb)
 	cudaFree(rb->huges_dev);
 	cudaFree(rb->counters_dev);
 	cudaFree(rb->scratch);
+	free(rb->bins);
+	free(rb->in_offsets);
+	free(rb->out_offsets);
 	free(rb);
 }
 
@@ -179,11 +186,12 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			goto fail;
 		}
 		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
-			const uint32_t tg = fsr_item_threads(&f->rp);
+			const fgk_plan *pl = f->rg_tuned && f->rg_dmem ? &f->rg_plan : &f->rp;
+			const uint32_t tg = f->rg_tuned ? f->rg_tg : fsr_item_threads(pl);
 			uint32_t G = FSR_THREADS / tg;
 			if (G * fsr_slots(L) > (uint32_t)fgk_tasks_slots())
 				G = (uint32_t)fgk_tasks_slots() / fsr_slots(L);
-			plans[nplans] = f->rp;
+			plans[nplans] = *pl;
 			cap_tasks += (j - i + G - 1) / G;
 			plans[nplans].threads = tg; /* reused below: threads per item */
 			plans[nplans].per_cta = G;  /* and items per task */
@@ -227,8 +235,8 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 				b->in_off = in_offsets[order[k].idx];
 				b->out_off = out_offsets[order[k].idx];
 				b->scratch_off = scratch_f2;
-				b->ls1 = fsr_lanes_log2(L1, L2);
-				b->ls2 = fsr_lanes_log2(L2, L1);
+				b->ls1 = f->rg_tuned ? f->rg_ls1 : fsr_lanes_log2(L1, L2);
+				b->ls2 = f->rg_tuned ? f->rg_ls2 : fsr_lanes_log2(L2, L1);
 				b->ncols = (L2 + (1u << b->ls1) - 1) >> b->ls1;
 				b->nrows = (L1 + (1u << b->ls2) - 1) >> b->ls2;
 				total_cols += b->ncols;
@@ -313,6 +321,15 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		goto cuda_fail;
 	if ((e = cudaStreamCreateWithFlags(&rb->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
 		goto cuda_fail;
+	rb->mod = modulation;
+	rb->bins = (unsigned *)malloc(sizeof(unsigned) * n);
+	rb->in_offsets = (size_t *)malloc(sizeof(size_t) * n);
+	rb->out_offsets = (size_t *)malloc(sizeof(size_t) * n);
+	if (!rb->bins || !rb->in_offsets || !rb->out_offsets)
+		goto fail;
+	memcpy(rb->bins, bins, sizeof(unsigned) * n);
+	memcpy(rb->in_offsets, in_offsets, sizeof(size_t) * n);
+	memcpy(rb->out_offsets, out_offsets, sizeof(size_t) * n);
 	free(order);
 	free(plans);
 	free(items);
@@ -477,4 +494,232 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 	}
 	f->tasks->op = op; /* the task list does not depend on the direction */
 	return fsr_record(f->tasks, out, in, stream);
+}
+
+/* ------------------------------------------------------------------------
+ * Autotuning the task schedule per size */
+
+/* Device tables of a whole-item chain candidate (the resident plan with a
+ * forced radix order); *dmem receives the allocation. */
+static int fsr_candidate_plan(struct fs_impl *fs, const struct fftset_fft *f, const uint32_t *rad, uint32_t n,
+                              fgk_plan *out, void **dmem)
+{
+	const uint32_t L = f->lfft;
+	size_t ntw;
+	float *h;
+	cudaError_t e;
+	if (fgk_plan_resident(out, L, f->rp.modulation, fs->max_smem, rad, n))
+		return FFTSET_E_UNSUPPORTED;
+	ntw = fgk_plan_twiddles(out, NULL);
+	h = (float *)malloc(sizeof(float) * 2 * (ntw ? ntw : 1));
+	if (!h)
+		return FFTSET_E_NOMEM;
+	fgk_plan_twiddles(out, h);
+	if ((e = cudaMalloc(dmem, sizeof(float) * 2 * (ntw ? ntw : 1))) != cudaSuccess) {
+		free(h);
+		cudaGetLastError();
+		return FFTSET_E_NOMEM;
+	}
+	e = cudaMemcpy(*dmem, h, sizeof(float) * 2 * ntw, cudaMemcpyHostToDevice);
+	free(h);
+	if (e != cudaSuccess) {
+		cudaFree(*dmem);
+		*dmem = NULL;
+		return FFTSET_E_CUDA;
+	}
+	out->tw = *dmem;
+	out->modtw = f->rp.modtw;
+	out->kidx = f->rp.kidx;
+	out->kvw = f->rp.kvw;
+	out->dev = NULL; /* the task kernel reads the plan from its own array */
+	return FFTSET_OK;
+}
+
+/* Times one launch schedule of `count` items of f's size (the current
+ * rg_* fields), best of a few launches. */
+static float fsr_time_size(struct fs_impl *fs, struct fftset_fft *f, int op, unsigned count, float *buf_in,
+                           float *buf_out, cudaEvent_t e0, cudaEvent_t e1)
+{
+	unsigned *bins = (unsigned *)malloc(sizeof(unsigned) * count);
+	size_t *offs = (size_t *)malloc(sizeof(size_t) * count);
+	struct fftset_ragged *rb;
+	float best = -1.f;
+	unsigned b;
+	int r;
+	if (!bins || !offs) {
+		free(bins);
+		free(offs);
+		return -1.f;
+	}
+	for (b = 0; b < count; b++) {
+		bins[b] = f->lfft;
+		offs[b] = (size_t)b * 2 * f->lfft;
+	}
+	rb = fsr_create(fs, f->modulator, op, count, bins, offs, offs);
+	free(bins);
+	free(offs);
+	if (!rb)
+		return -1.f;
+	if (fsr_record(rb, buf_out, buf_in, fs->stream) == 0) {
+		for (r = 0; r < 3; r++) {
+			float ms = 0.f;
+			cudaEventRecord(e0, fs->stream);
+			fsr_record(rb, buf_out, buf_in, fs->stream);
+			cudaEventRecord(e1, fs->stream);
+			if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+				break;
+			if (best < 0.f || ms < best)
+				best = ms;
+		}
+	}
+	cudaStreamSynchronize(fs->stream);
+	cudaGetLastError();
+	fsr_free(rb);
+	return best;
+}
+
+int fftset_ragged_autotune(struct fftset_ragged *rb)
+{
+	struct fs_impl *fs;
+	float *bin = NULL, *bout = NULL;
+	cudaEvent_t e0 = NULL, e1 = NULL;
+	unsigned i, maxL = 0;
+	size_t cap;
+	struct fftset_ragged *nrb;
+	int rc = FFTSET_OK;
+	if (!rb || !rb->bins)
+		return FFTSET_E_INVALID;
+	fs = rb->fs;
+	for (i = 0; i < rb->n; i++)
+		if (rb->bins[i] > maxL)
+			maxL = rb->bins[i];
+	/* timing buffers: 32 MB of items, at least two items of the largest size */
+	cap = (size_t)8 << 20;
+	if (cap < 4 * (size_t)maxL)
+		cap = 4 * (size_t)maxL;
+	if (cudaMalloc((void **)&bin, cap * sizeof(float)) != cudaSuccess ||
+	    cudaMalloc((void **)&bout, cap * sizeof(float)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+	    cudaEventCreate(&e1) != cudaSuccess) {
+		cudaGetLastError();
+		rc = fs_latch(fs, FFTSET_E_NOMEM, 0);
+		goto out;
+	}
+	cudaMemsetAsync(bin, 0, cap * sizeof(float), fs->stream);
+	for (i = 0; i < rb->n; i++) {
+		struct fftset_fft *f = fs_create_plan(fs, rb->mod, rb->bins[i]);
+		const uint32_t L = rb->bins[i];
+		const unsigned count = (unsigned)(cap / (2 * (size_t)L));
+		float best = -1.f, t;
+		if (!f || f->rg_tuned || L > 65536)
+			continue;
+		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
+			/* whole items: radix order x threads per item */
+			uint32_t rad[3][FGK_MAX_STAGES], nr[3], nc = 0, c, k, tgs[3], ntg, q;
+			fgk_plan best_plan = f->rp;
+			void *best_dmem = NULL;
+			uint32_t best_tg = fsr_item_threads(&f->rp);
+			nr[0] = f->rp.fwd.nstages;
+			for (k = 0; k < nr[0]; k++)
+				rad[0][k] = f->rp.fwd.st[k].radix;
+			nc = 1;
+			if (nr[0] > 1) { /* reversed order: smallest radix first */
+				nr[1] = nr[0];
+				for (k = 0; k < nr[0]; k++)
+					rad[1][k] = rad[0][nr[0] - 1 - k];
+				nc = 2;
+			}
+			for (c = 0; c < nc; c++) {
+				fgk_plan cand;
+				void *dm = NULL;
+				if (c == 0) {
+					cand = f->rp;
+				} else if (fsr_candidate_plan(fs, f, rad[c], nr[c], &cand, &dm) != FFTSET_OK) {
+					continue;
+				}
+				/* threads per item: narrowest stage, 2x that, widest stage */
+				tgs[0] = fsr_item_threads(&cand);
+				tgs[1] = tgs[0] * 2 > FSR_THREADS ? FSR_THREADS : tgs[0] * 2;
+				{
+					uint32_t s2, w = 1;
+					for (s2 = 0; s2 < cand.fwd.nstages; s2++)
+						if (L / cand.fwd.st[s2].radix > w)
+							w = L / cand.fwd.st[s2].radix;
+					w = (w + 31) & ~31u;
+					tgs[2] = w > FSR_THREADS ? FSR_THREADS : w;
+				}
+				ntg = 3;
+				for (q = 0; q < ntg; q++) {
+					if (q > 0 && (tgs[q] == tgs[q - 1] || (q == 2 && tgs[2] == tgs[0])))
+						continue;
+					f->rg_tuned = 1;
+					f->rg_plan = cand;
+					f->rg_dmem = c ? dm : NULL;
+					f->rg_tg = tgs[q];
+					t = fsr_time_size(fs, f, rb->op, count, bin, bout, e0, e1);
+					if (t > 0.f && (best < 0.f || t < best)) {
+						best = t;
+						best_plan = cand;
+						best_tg = tgs[q];
+						if (best_dmem && best_dmem != dm)
+							cudaFree(best_dmem);
+						best_dmem = c ? dm : NULL;
+					}
+				}
+				if (dm && dm != best_dmem)
+					cudaFree(dm);
+			}
+			f->rg_plan = best_plan;
+			f->rg_dmem = best_dmem;
+			f->rg_tg = best_tg;
+			f->rg_tuned = 1;
+		} else {
+			/* two-level items: lanes per COLS / ROWS tile (16 and up) */
+			uint32_t da, db, ls1m, ls2m, best1, best2;
+			if (fs_ensure_fourstep(fs, f) != FFTSET_OK)
+				continue;
+			ls1m = fsr_lanes_log2(f->p4.L1, f->p4.L2);
+			ls2m = fsr_lanes_log2(f->p4.L2, f->p4.L1);
+			best1 = ls1m;
+			best2 = ls2m;
+			for (da = 0; da < 2; da++)
+				for (db = 0; db < 2; db++) {
+					if (ls1m < 4 + da || ls2m < 4 + db)
+						continue;
+					f->rg_tuned = 1;
+					f->rg_ls1 = ls1m - da;
+					f->rg_ls2 = ls2m - db;
+					t = fsr_time_size(fs, f, rb->op, count, bin, bout, e0, e1);
+					if (t > 0.f && (best < 0.f || t < best)) {
+						best = t;
+						best1 = ls1m - da;
+						best2 = ls2m - db;
+					}
+				}
+			f->rg_ls1 = best1;
+			f->rg_ls2 = best2;
+			f->rg_tuned = 1;
+		}
+	}
+	/* rebuild this batch with the chosen schedules */
+	nrb = fsr_create(fs, rb->mod, rb->op, rb->n, rb->bins, rb->in_offsets, rb->out_offsets);
+	if (!nrb) {
+		rc = fs->err ? fs->err : FFTSET_E_NOMEM;
+		goto out;
+	}
+	{
+		struct fftset_ragged tmp = *rb;
+		nrb->use_graph = rb->use_graph;
+		*rb = *nrb;
+		*nrb = tmp; /* the old lists go with nrb */
+		nrb->exec = tmp.exec;
+		fsr_free(nrb);
+	}
+out:
+	if (e0)
+		cudaEventDestroy(e0);
+	if (e1)
+		cudaEventDestroy(e1);
+	cudaFree(bin);
+	cudaFree(bout);
+	return rc;
 }

@@ -177,6 +177,13 @@ int      fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, con
 int      fftset_ragged_set_graph(struct fftset_ragged *rb, int enable);
 double   fftset_ragged_bytes(const struct fftset_ragged *rb);  /* one read + one write of every item */
 unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb);
+/* Per-size schedule autotuner of the task kernel: for every distinct size of
+ * rb up to 65536 bins, times candidate schedules on scratch buffers (whole
+ * items: radix order, as planned or reversed, x threads per item, which sets
+ * the items per task; two-level items: lanes per column / row tile) and keeps
+ * the fastest on the size's plan (later batches of the same fftset reuse
+ * it), then rebuilds rb's task list. */
+int      fftset_ragged_autotune(struct fftset_ragged *rb);
 void     fftset_ragged_destroy(struct fftset_ragged *rb);
 
 /* Adjoint of fftset_fft_conv (the reference has only the forward,

@@ -84,3 +84,38 @@ def test_ragged_rejects_bad_input(fftset_lib, gpu_set):
     with pytest.raises(fftset_lib.FftsetError):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64], [1], [0])
 
+
+
+def test_ragged_autotune_keeps_results(fftset_lib):
+    """fftset_ragged_autotune picks per-size schedules (radix order, threads
+    per item, lanes per tile) by timing and rebuilds the batch: the results
+    stay within tolerance of FP64, before and after, graph replay included."""
+    import torch
+    S = fftset_lib.FftSet()
+    try:
+        sizes = [60, 96, 243, 1024, 1536, 4096, 6144, 16384, 59049, 65536, 131072]
+        sizes = sizes + sizes[::-1][1:]
+        offs, total = layout(sizes)
+        rng = np.random.default_rng(21)
+        x = rng.uniform(-1, 1, total).astype(np.float32)
+        xd = torch.from_numpy(x).cuda()
+        S.set_stream(torch.cuda.current_stream())
+        for mod, op in ((0, fftset_lib.OP_FORWARD), (1, fftset_lib.OP_INVERSE)):
+            rb = fftset_lib.Ragged(S, mod, op, sizes, offs, offs)
+            y0 = torch.full_like(xd, 3.0)
+            rb.execute(y0, xd)
+            rb.autotune()
+            y1 = torch.full_like(xd, 3.0)
+            rb.execute(y1, xd)
+            rb.execute(y1, xd)
+            torch.cuda.synchronize()
+            a, b = y0.cpu().numpy(), y1.cpu().numpy()
+            for L, o in zip(sizes, offs):
+                xi = x[o:o + 2 * L]
+                want = O.forward64(mod, xi) if op == fftset_lib.OP_FORWARD else O.inverse64(mod, xi)
+                assert O.rel_l2(a[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (L, "before")
+                assert O.rel_l2(b[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (L, "after")
+                assert np.all(b[o + 2 * L:o + 2 * L + 2] == 3.0)
+            rb.close()
+    finally:
+        S.close()
