@@ -79,6 +79,7 @@ _decl("fftset_ragged_bytes", C.c_double, [_vp])
 _decl("fftset_ragged_persistent_items", _u, [_vp])
 _decl("fftset_ragged_destroy", None, [_vp])
 _decl("fftset_ragged_autotune", C.c_int, [_vp])
+_decl("fftset_fft_conv_overlap_add", C.c_int, [_vp, _vp, _vp, _sz, _vp, _u, _u])
 _decl("fftset_fft_conv_adjoint_batch", C.c_int, [_vp, _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _u])
 
 MODULATION_COMPLEX = _vp.in_dll(_lib, "FFTSET_MODULATION_COMPLEX").value
@@ -203,15 +204,16 @@ class FftSet:
         if not h:
             self.clear_error()
             return None
-        return self._plans.setdefault(h, Fft(self, h))
+        return self._plans.setdefault(h, Fft(self, h, _mod_ptr(modulation) == MODULATION_COMPLEX))
 
 
 class Fft:
     """One plan: a `const struct fftset_fft *`."""
 
-    def __init__(self, owner: FftSet, handle: int):
+    def __init__(self, owner: FftSet, handle: int, is_complex: bool = False):
         self.owner = owner
         self.handle = handle
+        self.is_complex = is_complex
         self.bins = int(_lib.fftset_fft_bins(handle))
         self.kernel_lanes = int(_lib.fftset_fft_kernel_lanes(handle))
 
@@ -297,6 +299,21 @@ class Fft:
 
     def conv_batch(self, out, inp, kern):
         return self._batch(_lib.fftset_fft_conv_batch, out, inp, kern)
+
+    def conv_overlap_add(self, out, inp, kern, kernel_length: int, block_length: int = 0):
+        """fftset_fft_conv_overlap_add: out (samples + kernel_length - 1
+        samples) = complex_bins x the linear convolution of inp with the
+        kernel whose spectrum is kern. Samples are floats (FREQ_OFFSET_REAL)
+        or interleaved complex pairs (COMPLEX)."""
+        self._sync_stream(out, inp, kern)
+        n = int(inp.numel() if hasattr(inp, "numel") else inp.size)
+        samples = n // 2 if self.is_complex else n
+        rc = _lib.fftset_fft_conv_overlap_add(self.handle, _ptr(out), _ptr(inp), samples, _ptr(kern),
+                                              kernel_length, block_length)
+        if rc:
+            self.owner.check()
+            raise FftsetError(error_string(rc))
+        return out
 
     def conv_adjoint_batch(self, grad_input, grad_taps, grad_out, inp, kern):
         """fftset_fft_conv_adjoint_batch: gradients of sum_b <grad_out_b, y_b>

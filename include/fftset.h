@@ -201,6 +201,23 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
                                   float *grad_taps, const float *grad_output, size_t go_stride,
                                   const float *input_buf, size_t in_stride, const float *kernel_buf, unsigned count);
 
+/* Overlap-add block convolution (the reference leaves this loop to its
+ * callers; its README.md:3 use case, block and transform lengths as from
+ * fftset_recommend_conv_length, src/fftset.c:145-167): the linear
+ * convolution of `samples` input samples (reals for FREQ_OFFSET_REAL,
+ * interleaved complex for COMPLEX) with a kernel of kernel_length taps whose
+ * spectrum kernel_buf comes from fftset_fft_conv_get_kernel of the taps
+ * zero-padded to the plan's length N (2 complex_bins reals, or complex_bins
+ * complex points). The input is cut into blocks of block_length samples (0:
+ * N - kernel_length + 1, the most that does not wrap), each zero-padded to N;
+ * one batched convolution; the results are overlap-added into output_buf,
+ * samples + kernel_length - 1 samples, complex_bins times the linear
+ * convolution (the scale of fftset_fft_conv). Device buffers; uses 2 x
+ * blocks x N samples of the fftset's staging memory. */
+int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf, const float *input_buf,
+                                size_t samples, const float *kernel_buf, unsigned kernel_length,
+                                unsigned block_length);
+
 /* No counterpart in the reference. A batched call (op FFTSET_OP_*, the
  * arguments of fftset_fft_*_batch) that allocates nothing, for callers that
  * must not call cudaMalloc while they run: a real-time audio callback with a

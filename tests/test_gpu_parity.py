@@ -493,3 +493,40 @@ def test_pinned_host_buffers_in_place_access(gpu_set, mod, L, op):
     call(y, y, K)
     assert O.rel_l2(y.numpy()[:, :2 * L], w) <= 1e-6
     assert np.array_equal(y.numpy()[:, 2 * L:], x.numpy()[:, 2 * L:])
+
+
+@pytest.mark.parametrize("mod,L,K,blk", [(1, 1536, 401, 0), (1, 1536, 2048, 0), (1, 4096, 900, 1000),
+                                         (0, 1024, 200, 0), (1, 768, 1, 0)])
+def test_overlap_add_linear_convolution(gpu_set, mod, L, K, blk):
+    """fftset_fft_conv_overlap_add: complex_bins times the linear convolution
+    of a long signal (several hundred blocks, ragged last block) with a K-tap
+    kernel, against FP64 np.convolve."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    N = L if mod == 0 else 2 * L
+    rng = np.random.default_rng(L + K)
+    n = 97 * N + 13
+    if mod == 1:
+        x = rng.standard_normal(n).astype(np.float32)
+        taps = (rng.standard_normal(K) * np.exp(-np.arange(K) / max(K / 4, 1))).astype(np.float32)
+        h = np.zeros(N, np.float32)
+        h[:K] = taps
+        want = L * np.convolve(x.astype(np.float64), taps.astype(np.float64))
+        xin = x
+    else:
+        xc = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        tc = rng.standard_normal(K) + 1j * rng.standard_normal(K)
+        h = np.zeros(2 * N, np.float32)
+        h[0:2 * K:2], h[1:2 * K:2] = tc.real, tc.imag
+        wc = L * np.convolve(xc.astype(np.complex64).astype(np.complex128), tc.astype(np.complex64).astype(np.complex128))
+        want = np.empty(2 * wc.size)
+        want[0::2], want[1::2] = wc.real, wc.imag
+        xin = np.empty(2 * n, np.float32)
+        xin[0::2], xin[1::2] = xc.real, xc.imag
+    K_spec = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K_spec, dev(h))
+    out = torch.full((want.size + 4,), float("nan"), device="cuda")
+    f.conv_overlap_add(out[:want.size], dev(xin), K_spec, K, blk)
+    got = host(out)
+    assert O.rel_l2(got[:want.size], want) <= tol(mod, L)
+    assert np.all(np.isnan(got[want.size:]))
