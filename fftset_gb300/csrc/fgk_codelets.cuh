@@ -1,8 +1,8 @@
 /* Register-resident DFT codelets (forward sign, natural order in and out).
  *
  * dft<R>(v) replaces v[0..R) by X[k] = sum_p v[p] e^{-j 2 pi p k / R}.
- * Radices 2, 3, 4, 5, 8 are written out; 16 is 4x4 Cooley-Tukey with its
- * internal twiddles written as constants; 6, 10, 12 and 15 are Good-Thomas
+ * Radices 2, 3, 4, 5, 8 are written out; 9 and 16 are 3x3 and 4x4
+ * Cooley-Tukey with their internal twiddles written as constants; 6, 10, 12 and 15 are Good-Thomas
  * prime-factor composites (coprime factors, no internal twiddles, the index
  * maps are compile-time register renamings). These play the role of the
  * reference's radix butterflies (src/fftset_vec.c:109-845) but are this
@@ -67,6 +67,12 @@ FGK_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); 
 #define FGK_C2_5    0.80901699437494742410f  /* -cos(4pi/5) */
 #define FGK_S1_5    0.95105651629515357212f  /* sin(2pi/5) */
 #define FGK_S2_5    0.58778525229247312917f  /* sin(4pi/5) */
+#define FGK_C1_9    0.76604444311897803520f  /* cos(2pi/9) */
+#define FGK_S1_9    0.64278760968653932632f  /* sin(2pi/9) */
+#define FGK_C2_9    0.17364817766693034885f  /* cos(4pi/9) */
+#define FGK_S2_9    0.98480775301220805936f  /* sin(4pi/9) */
+#define FGK_C4_9    0.93969262078590838405f  /* -cos(8pi/9) */
+#define FGK_S4_9    0.34202014332566873304f  /* sin(8pi/9) */
 
 FGK_HD void dft2(float2 &a, float2 &b)
 {
@@ -132,6 +138,28 @@ FGK_HD void dft8(float2 *v)
 	v[1] = t0; v[3] = t1; v[5] = t2; v[7] = t3;
 }
 
+/* 9 = 3 x 3: column DFT3 over n1 of v[3 n1 + n2], twiddle w9^{n2 k1}, row
+ * DFT3 over n2, X[k1 + 3 k2]. */
+FGK_HD void dft9(float2 *v)
+{
+	float2 a0 = v[0], a1 = v[3], a2 = v[6];
+	float2 b0 = v[1], b1 = v[4], b2 = v[7];
+	float2 c0 = v[2], c1 = v[5], c2 = v[8];
+	dft3(a0, a1, a2);
+	dft3(b0, b1, b2);
+	dft3(c0, c1, c2);
+	b1 = cmul(b1, make_float2(FGK_C1_9, -FGK_S1_9));  /* w9^1 */
+	b2 = cmul(b2, make_float2(FGK_C2_9, -FGK_S2_9));  /* w9^2 */
+	c1 = cmul(c1, make_float2(FGK_C2_9, -FGK_S2_9));  /* w9^2 */
+	c2 = cmul(c2, make_float2(-FGK_C4_9, -FGK_S4_9)); /* w9^4 */
+	dft3(a0, b0, c0);
+	dft3(a1, b1, c1);
+	dft3(a2, b2, c2);
+	v[0] = a0; v[3] = b0; v[6] = c0;
+	v[1] = a1; v[4] = b1; v[7] = c1;
+	v[2] = a2; v[5] = b2; v[8] = c2;
+}
+
 /* 16 = 4 x 4: column DFT4 over p2 of v[p1 + 4 p2], twiddle w16^{p1 k2},
  * row DFT4 over p1, X[4 k1 + k2]. */
 FGK_HD void dft16(float2 *v)
@@ -175,6 +203,7 @@ template <> struct Radix<3> { static FGK_HD void run(float2 *v) { dft3(v[0], v[1
 template <> struct Radix<4> { static FGK_HD void run(float2 *v) { dft4(v[0], v[1], v[2], v[3]); } };
 template <> struct Radix<5> { static FGK_HD void run(float2 *v) { dft5(v[0], v[1], v[2], v[3], v[4]); } };
 template <> struct Radix<8> { static FGK_HD void run(float2 *v) { dft8(v); } };
+template <> struct Radix<9> { static FGK_HD void run(float2 *v) { dft9(v); } };
 template <> struct Radix<16> { static FGK_HD void run(float2 *v) { dft16(v); } };
 
 /* Good-Thomas prime-factor composite for N = A*B, gcd(A,B) = 1:

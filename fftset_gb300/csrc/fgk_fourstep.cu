@@ -43,6 +43,7 @@ enum { FGK4_OUT_FORWARD = 0, FGK4_OUT_FINAL = 1, FGK4_OUT_KERNEL = 2, FGK4_OUT_P
 	case 5: { constexpr int R_ = 5; CALL; } break;                  \
 	case 6: { constexpr int R_ = 6; CALL; } break;                  \
 	case 8: { constexpr int R_ = 8; CALL; } break;                  \
+	case 9: { constexpr int R_ = 9; CALL; } break;                  \
 	case 10: { constexpr int R_ = 10; CALL; } break;                \
 	case 12: { constexpr int R_ = 12; CALL; } break;                \
 	case 15: { constexpr int R_ = 15; CALL; } break;                \

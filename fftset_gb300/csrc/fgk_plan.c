@@ -24,7 +24,7 @@ static const struct {
 } FGK_RADIX[] = {
 	{16, 4, 0, 0, 195}, {15, 0, 1, 1, 217}, {12, 2, 1, 0, 188}, {10, 1, 0, 1, 182},
 	{8, 3, 0, 0, 162},  {6, 1, 1, 0, 163},  {5, 0, 0, 1, 160},  {4, 2, 0, 0, 125},
-	{3, 0, 1, 0, 133},  {2, 1, 0, 0, 90},
+	{3, 0, 1, 0, 133},  {2, 1, 0, 0, 90},   {9, 0, 2, 0, 218},
 };
 #define FGK_NRADIX (sizeof(FGK_RADIX) / sizeof(FGK_RADIX[0]))
 
@@ -101,7 +101,7 @@ static int factor235(uint32_t L, uint32_t *a, uint32_t *b, uint32_t *c)
  * shared-memory bank conflicts under the i + i/16 padding. */
 /* radix sets: all codelets, or only those whose register tile divides a
  * 16/32-element budget well (used when the full set needs > 1024 threads) */
-#define FGK_ALL_RADICES 0x3ffu
+#define FGK_ALL_RADICES 0x7ffu
 #define FGK_SMALL_RADICES ((1u << 0) | (1u << 4) | (1u << 6) | (1u << 7) | (1u << 8) | (1u << 9))
 
 static int plan_chain_set(uint32_t L, uint32_t allowed, uint32_t *radices, uint32_t *nstages)

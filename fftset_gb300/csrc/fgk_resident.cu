@@ -41,6 +41,7 @@ namespace fgk {
 	case 5: { constexpr int R_ = 5; CALL; } break;                  \
 	case 6: { constexpr int R_ = 6; CALL; } break;                  \
 	case 8: { constexpr int R_ = 8; CALL; } break;                  \
+	case 9: { constexpr int R_ = 9; CALL; } break;                  \
 	case 10: { constexpr int R_ = 10; CALL; } break;                \
 	case 12: { constexpr int R_ = 12; CALL; } break;                \
 	case 15: { constexpr int R_ = 15; CALL; } break;                \

@@ -354,6 +354,34 @@ def test_autotune_picks_a_working_kernel(fftset_lib, gpu_set):
     assert O.rel_l2(host(y), O.conv64(1, x, h)) <= tol(1, 1536)
 
 
+RADIX9 = [(0, 81), (1, 243), (0, 729), (1, 2187), (0, 3888), (1, 6561), (0, 19683)]
+
+
+@pytest.mark.parametrize("mod,L", RADIX9)
+def test_radix9_chains_against_fp64(gpu_set, mod, L):
+    """Resident sizes whose radix chains use the radix-9 codelet (81 = 9 9,
+    19683 = 9 9 9 9 3, 3888 = 12 12 9 3): forward, inverse and conv of a
+    batch of 3 against FP64."""
+    import torch
+    f = gpu_set.create_fft(mod, L)
+    assert f is not None
+    rng = np.random.default_rng(L + 7 * mod)
+    x = rng.standard_normal((3, 2 * L)).astype(np.float32)
+    X = torch.empty(3, 2 * L, device="cuda")
+    f.forward_batch(X, dev(x))
+    Xh = host(X)
+    assert O.rel_l2(Xh, O.forward64(mod, x)) <= tol(mod, L)
+    r = torch.empty_like(X)
+    f.inverse_batch(r, X)
+    assert O.rel_l2(host(r), O.inverse64(mod, Xh)) <= tol(mod, L)
+    h = rng.standard_normal(2 * L).astype(np.float32)
+    K = torch.empty(2 * L, device="cuda")
+    f.conv_get_kernel(K, dev(h))
+    y = torch.empty_like(X)
+    f.conv_batch(y, dev(x), K)
+    assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
+
+
 FOURSTEP = [32768, 36864, 46656, 59049, 65536, 131072, 393216]
 
 
