@@ -709,7 +709,7 @@ int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, c
                      unsigned count, size_t in_stride, size_t out_stride)
 {
 	if (f->fourstep && (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE)) {
-		/* tile tasks (fgk_tasks.cu): two- or three-level split */
+		/* tile tasks (fgk_tasks.cuh): two- or three-level split */
 		const int rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, f->fs->stream);
 		if (rc != -FFTSET_E_UNSUPPORTED)
 			return rc;

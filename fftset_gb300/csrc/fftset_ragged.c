@@ -3,7 +3,7 @@
  *
  * fsr_create plans every distinct size through the fftset's own plan cache
  * (so all sizes share the fftset's twiddle tables) and builds the task list
- * of one persistent launch (fgk_tasks.cu), every task a tile of at most
+ * of one persistent launch (fgk_tasks.cuh), every task a tile of at most
  * fgk_tasks_points() points:
  *   - items up to fgk_tasks_points() bins: SMALL tasks of same-size items;
  *   - items up to 65536 bins: their four-step split L = L1 L2 (both <= 256),

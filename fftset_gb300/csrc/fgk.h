@@ -80,7 +80,7 @@ typedef struct fgk_plan4 {
 } fgk_plan4;
 
 /* Plan of a three-level transform L = L1 L2 L3 (each <= 256, L1 >= 16) run
- * as tile tasks (fgk_tasks.cu): n = (n1 L2 + n2) L3 + n3,
+ * as tile tasks (fgk_tasks.cuh): n = (n1 L2 + n2) L3 + n3,
  * k = k1 + L1 (k2 + L2 k3).
  *   pass A: DFT_L1 over n1, times w_{L1 L2}^{n2 k1}, into A[k1][n2 L3 + n3];
  *   pass B: DFT_L2 over n2, times w_L^{n3 (k1 + L1 k2)}, into
@@ -105,7 +105,7 @@ typedef struct fgk_rg_item {
 	uint64_t in_off, out_off;
 } fgk_rg_item;
 
-/* Ragged batches as tasks of one persistent launch (fgk_tasks.cu). Every
+/* Ragged batches as tasks of one persistent launch (fgk_tasks.cuh). Every
  * task is a tile of at most fgk_tasks_points() points:
  *   SMALL  n same-size items (whole transforms, tg threads each);
  *   COLS   lanes of columns of a big item's four-step split L = L1 L2 (DFTs

@@ -1,0 +1,673 @@
+/* Ragged batches as one persistent launch of tile tasks.
+ *
+ * Every task is a tile of at most FGKT_POINTS points held in two padded
+ * shared-memory buffers (ping-pong Stockham stages, one butterfly per thread
+ * at a time, runtime radix; fgk_pingpong.cuh), so one CTA of 256 threads
+ * needs 70 KB and three CTAs share an SM: while one loads its tile from HBM
+ * the others compute, which is what keeps enough bytes in flight. Loads are
+ * issued eight per thread before any is used.
+ *
+ *   SMALL  n items of one size L <= FGKT_POINTS, whole transforms side
+ *          by side (tg threads each), HBM in, HBM out.
+ *   COLS   a big item (L > FGKT_POINTS) split L = L1 L2 (the fftset's
+ *          four-step plan: n = L2 n1 + n2, k = k1 + L1 k2): 2^ls1 adjacent
+ *          columns n2, each a DFT of length L1 over n1 whose first stage
+ *          reads the input directly (row segments of 2^ls1 elements) and
+ *          whose last stage multiplies by w_L^{n2 k1} and writes the item's
+ *          scratch directly, in the order the ROWS tiles read it.
+ *   ROWS   2^ls2 adjacent rows k1 of that scratch (one contiguous block),
+ *          DFTs of length L2 over n2, the last stage writing X[k1 + L1 k2]
+ *          directly (segments of 2^ls2 elements).
+ * Only the middle stages of a big-item tile go through shared memory.
+ * Big-item tiles have at least 16 lanes (L1, L2 <= 256), which makes the
+ * Rows layout below conflict-free.
+ *
+ * A ROWS task waits for all COLS tasks of its item: each COLS task bumps the
+ * item's counter after its stores are visible (threadfence), and a ROWS task
+ * spins on it with a bounded wait (on timeout it raises the error flag and
+ * skips the tile). Tasks are claimed in list order from an atomic counter,
+ * and the host lists every COLS task of an item before its ROWS tasks, so a
+ * ROWS task only ever waits on tasks already claimed by running CTAs: no
+ * deadlock whatever the residency. The scratch of an item is written and
+ * read back within a few microseconds, so it is served by L2; the ROWS task
+ * discards the lines it has consumed (discard.global.L2) so that they are
+ * never written back to HBM.
+ *
+ * The FREQ_OFFSET_REAL modulation is fused into the loads (pack and
+ * e^{-j pi n/(2L)} = m1[n1] m2[n2]) and the final stores (split X[2m] = W[m],
+ * X[2(L-1-m)+1] = conj W[m]; inverse: y = Re/Im of u e^{-j pi m/(2L)}). */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fgk.h"
+#include "fgk_pingpong.cuh"
+
+namespace fgk {
+
+#ifndef FGKT_POINTS
+#define FGKT_POINTS 4096 /* points of a tile */
+#endif
+#ifndef FGKT_THREADS
+#define FGKT_THREADS 256 /* threads of a task CTA */
+#endif
+#ifndef FGKT_MIN_CTAS
+#define FGKT_MIN_CTAS 3 /* resident CTAs per SM the registers are budgeted for */
+#endif
+constexpr int TK_THREADS = FGKT_THREADS;
+/* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
+constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
+constexpr uint32_t TK_SPIN_LIMIT = 1u << 22;                         /* x 256 ns: about a second */
+
+/* q = w / d for 0 <= w < 2^24, inv = 1/d (one correction step) */
+__device__ __forceinline__ int tk_div(int w, int d, float inv)
+{
+	int q = __float2int_rz(__int2float_rn(w) * inv);
+	const int r = w - q * d;
+	if (r < 0)
+		q--;
+	else if (r >= d)
+		q++;
+	return q;
+}
+
+/* Shared-memory layouts of a tile (element i of lane l):
+ *   Pad   (one lane, whole items)  slot i + i/16: the strided accesses of a
+ *         stage spread over the banks;
+ *   Rows  (16 or more lanes)       slot i (nl + 1) + l: linear in i, so a
+ *         stage's R accesses are one base plus multiples of a stride, and
+ *         conflict-free whether a warp runs along the lanes or along i. */
+struct Pad {
+	int ls;
+	__device__ __forceinline__ int slot(int i, int lane) const { return rslot((i << ls) + lane); }
+};
+struct Rows {
+	int ls;
+	__device__ __forceinline__ int slot(int i, int lane) const { return i * ((1 << ls) + 1) + lane; }
+};
+
+/* Stockham stage over a lane-interleaved tile: element i of lane l at
+ * rslot((i << ls) + l); work item w = (butterfly j, lane) with the lane
+ * fastest, so a warp's accesses are consecutive slots. */
+template <int R, class A>
+__device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int Lp, int ls, int ns,
+                                           const float2 *__restrict__ tw, int tid, int T, A ad)
+{
+	const int nbf = Lp / R;
+	const int items = nbf << ls;
+	const int lm = (1 << ls) - 1;
+	for (int w = tid; w < items; w += T) {
+		const int j = w >> ls, lane = w & lm;
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = src[ad.slot(j + p * nbf, lane)];
+		const int k = j % ns;
+		if (ns > 1) {
+			const float2 *t = tw + k * (R - 1);
+#pragma unroll
+			for (int p = 1; p < R; p++)
+				v[p] = cmul(v[p], __ldg(t + p - 1));
+		}
+		Radix<R>::run(v);
+		const int base = (j - k) * R + k;
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			dst[ad.slot(base + q * ns, lane)] = v[q];
+	}
+}
+
+/* ---- tiles: first and last stages straight from and to memory ---------- */
+/* First stage of a tile (ns = 1, no twiddles) straight from memory:
+ * butterfly j of lane l reads ld(j + p nbf, l) (lanes fastest, so a warp
+ * reads consecutive lanes of one element: the row segments in memory). */
+/* butterflies a thread loads side by side in the first stage, so that
+ * 16 loads are in flight for the radices 2, 4 and 8 */
+template <int R> struct Batch {
+	static constexpr int B = 1;
+};
+
+template <int R, class A, class Ld>
+__device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls, int tid, int T, A ad)
+{
+	constexpr int B = Batch<R>::B;
+	const int nbf = Lp / R;
+	const int items = nbf << ls;
+	const int lm = (1 << ls) - 1;
+	for (int w0 = tid; w0 < items; w0 += B * T) {
+		float2 v[B][R];
+#pragma unroll
+		for (int b = 0; b < B; b++) {
+			const int w = w0 + b * T;
+			if (w < items) {
+				const int j = w >> ls, lane = w & lm;
+#pragma unroll
+				for (int p = 0; p < R; p++)
+					v[b][p] = ld(j + p * nbf, lane);
+			}
+		}
+#pragma unroll
+		for (int b = 0; b < B; b++) {
+			const int w = w0 + b * T;
+			if (w < items) {
+				const int j = w >> ls, lane = w & lm;
+				Radix<R>::run(v[b]);
+#pragma unroll
+				for (int q = 0; q < R; q++)
+					dst[ad.slot(j * R + q, lane)] = v[b][q];
+			}
+		}
+	}
+}
+
+/* Last stage of a tile (ns = Lp/R: butterfly j twiddled by w^{p j},
+ * outputs k = j + q nbf) straight to memory through st(j, q, nbf, lane, v). JF: a warp
+ * takes consecutive butterflies j of one lane (consecutive outputs k),
+ * otherwise consecutive lanes of one butterfly. */
+template <int R, bool JF, class A, class St>
+__device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, int ls, const float2 *__restrict__ tw,
+                                          int tid, int T, A ad)
+{
+	const int nbf = Lp / R;
+	const int items = nbf << ls;
+	const int lm = (1 << ls) - 1;
+	const float inv = 1.0f / (float)nbf;
+	for (int w = tid; w < items; w += T) {
+		int j, lane;
+		if (JF) {
+			lane = tk_div(w, nbf, inv);
+			j = w - lane * nbf;
+		} else {
+			j = w >> ls;
+			lane = w & lm;
+		}
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = src[ad.slot(j + p * nbf, lane)];
+		if (nbf > 1) {
+			const float2 *t = tw + j * (R - 1);
+#pragma unroll
+			for (int p = 1; p < R; p++)
+				v[p] = cmul(v[p], __ldg(t + p - 1));
+		}
+		Radix<R>::run(v);
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			st(j, q, nbf, lane, v[q]);
+	}
+}
+
+/* A single-stage chain (Lp = R): memory to memory */
+template <int R, class Ld, class St>
+__device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, int T)
+{
+	const int lanes = 1 << ls;
+	for (int lane = tid; lane < lanes; lane += T) {
+		float2 v[R];
+#pragma unroll
+		for (int p = 0; p < R; p++)
+			v[p] = ld(p, lane);
+		Radix<R>::run(v);
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			st(0, q, 1, lane, v[q]);
+	}
+}
+
+/* The whole chain of a tile: first stage from ld, middle stages in shared
+ * memory (A/B ping-pong), last stage to st. `after_first` runs once the first
+ * stage is done (all of its reads have returned). Threads with active ==
+ * false only take part in the barriers. */
+template <bool JF, class AD, class Ld, class St, class After>
+__device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw, int Lp, int ls, float2 *A,
+                                           float2 *B, int tid, int T, bool active, Ld &&ld, St &&st,
+                                           After &&after_first)
+{
+	const AD ad{ls};
+	const int n = (int)ch->nstages;
+	if (n == 1) {
+		if (active)
+			FGKR_RADIX_SWITCH(ch->st[0].radix, (lane_single<R_>(ld, st, ls, tid, T)));
+		__syncthreads();
+		after_first();
+		return;
+	}
+	if (active) {
+		const fgk_stage st0 = ch->st[0];
+		FGKR_RADIX_SWITCH(st0.radix, (lane_first<R_>(ld, A, Lp, ls, tid, T, ad)));
+	}
+	__syncthreads();
+	after_first();
+	float2 *src = A, *dst = B;
+	for (int s = 1; s < n - 1; s++) {
+		const fgk_stage sm = ch->st[s];
+		if (active)
+			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tw + sm.tw_off, tid, T, ad)));
+		__syncthreads();
+		float2 *t = src;
+		src = dst;
+		dst = t;
+	}
+	if (active) {
+		const fgk_stage sl = ch->st[n - 1];
+		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tw + sl.tw_off, tid, T, ad)));
+	}
+}
+
+/* Bounded wait of a whole CTA until *ctr >= need (thread 0 polls with an
+ * acquire load, then a barrier). On timeout the error flag is raised and
+ * false returned: the caller skips its tile. */
+__device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int *failed)
+{
+	if (threadIdx.x == 0) {
+		int f = 0;
+		uint32_t it = 0;
+		for (;;) {
+			int d;
+			asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(d) : "l"(ctr) : "memory");
+			if (d >= need)
+				break;
+			if (++it > TK_SPIN_LIMIT) {
+				f = 1;
+				if (err)
+					atomicExch(err, 1);
+				break;
+			}
+			__nanosleep(256);
+		}
+		__threadfence();
+		*failed = f;
+	}
+	__syncthreads();
+	return !*failed;
+}
+
+/* A tile's scratch stores, then one gpu-scope release of its count */
+__device__ __forceinline__ void tk_signal(int *ctr)
+{
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		__threadfence();
+		atomicAdd(ctr, 1);
+	}
+}
+
+/* ---- SMALL: whole items side by side ---------------------------------- */
+/* n items of one size, tg threads each (group g = threadIdx / tg), each
+ * group's first stage reading its item and its last stage writing its
+ * output directly. */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *__restrict__ plans,
+                                           const fgk_rg_item *__restrict__ items, const float *in_base,
+                                           float *out_base, float2 *smem)
+{
+	const fgk_plan *pl = plans + tk.ref;
+	const int L = (int)pl->L;
+	const int n = (int)(tk.b & 0xffff), T = (int)(tk.b >> 16);
+	const int g = (int)threadIdx.x / T;
+	const int tid = (int)threadIdx.x - g * T;
+	const bool active = g < n;
+	float2 *buf0 = smem + (size_t)(active ? g : 0) * 2 * rslots(L);
+	const fgk_rg_item it = active ? items[tk.a + g] : fgk_rg_item{0, 0};
+	const float *x = in_base + it.in_off;
+	const float2 *X = reinterpret_cast<const float2 *>(x);
+	float *y = out_base + it.out_off;
+	float2 *y2 = reinterpret_cast<float2 *>(y);
+	const float2 *mod = (const float2 *)pl->modtw;
+	const int hc = (L + 1) >> 1;
+	auto ld = [&](int i, int) {
+		if (!inverse) {
+			if (freq)
+				return cmul(make_float2(__ldcs(x + i), -__ldcs(x + L + i)), __ldg(mod + i));
+			return __ldcs(X + i);
+		}
+		/* conj W[i]: W[i] = X[2i] for i < ceil(L/2), conj X[2(L-1-i)+1] after */
+		if (freq)
+			return i < hc ? conjf2(__ldcs(X + 2 * i)) : __ldcs(X + 2 * (L - 1 - i) + 1);
+		return conjf2(__ldcs(X + i));
+	};
+	auto st = [&](int j, int q, int nbf, int, float2 v) {
+		const int k = j + q * nbf;
+		if (!inverse) {
+			if (!freq)
+				__stcs(y2 + k, v);
+			else if (k < hc)
+				__stcs(y2 + 2 * k, v);
+			else
+				__stcs(y2 + 2 * (L - 1 - k) + 1, conjf2(v));
+		} else if (freq) {
+			const float2 r = cmul(v, __ldg(mod + k));
+			__stcs(y + k, r.x);
+			__stcs(y + L + k, r.y);
+		} else {
+			__stcs(y2 + k, conjf2(v));
+		}
+	};
+	tile_chain<false, Pad>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
+	                       [] {});
+}
+
+/* COLS: columns n2base .. n2base + 2^ls1 - 1, DFTs of length L1 from the
+ * input into the item's scratch, which is laid out by ROWS tiles: element
+ * (k1, n2) at ((k1 >> ls2) L2 + n2) 2^ls2 + (k1 & (2^ls2 - 1)), so a ROWS
+ * tile reads one contiguous block with its lanes fastest. */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, const float *in_base,
+                                          float2 *scratch, int *done, float2 *smem)
+{
+	const fgk_plan4 *p = bg.p4;
+	const int L1 = (int)p->L1, L2 = (int)p->L2;
+	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
+	const int ls = (int)bg.ls1;
+	const int ls2 = (int)bg.ls2, lm2 = (1 << ls2) - 1;
+	const int n2base = (int)(tk.a << ls);
+	const float *x = in_base + bg.in_off;
+	const float2 *x2 = reinterpret_cast<const float2 *>(x);
+	const float2 *m1 = (const float2 *)p->m1, *m2 = (const float2 *)p->m2;
+	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo;
+	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
+	float2 *S = scratch + bg.scratch_off;
+	auto ld = [&](int n1, int lane) {
+		const int n2 = n2base + lane;
+		if (n2 >= L2)
+			return make_float2(0.f, 0.f);
+		const uint32_t n = (uint32_t)n1 * (uint32_t)L2 + (uint32_t)n2;
+		if (!inverse) {
+			if (freq)
+				return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), cmul(__ldg(m1 + n1), __ldg(m2 + n2)));
+			return __ldcs(x2 + n);
+		}
+		if (freq)
+			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
+		return conjf2(__ldcs(x2 + n));
+	};
+	const float2 *tq = (const float2 *)p->tq;
+	/* w_L^{n2 k1}, k1 = j + q nbf: w_L^{n2 j} w_{R L2}^{n2 q} (L = R nbf L2;
+	 * n2 q < R L2, so no reduction) */
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const int n2 = n2base + lane;
+		if (n2 >= L2)
+			return;
+		const int k1 = j + q * nbf;
+		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
+		const float2 a = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 w = q ? cmul(a, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : a;
+		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
+		       cmul(v, w));
+	};
+	tile_chain<true, Rows>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                       (int)blockDim.x, true, ld, st, [] {});
+	tk_signal(done);
+}
+
+/* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
+ * into X[k1 + L1 k2] */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, float *out_base, float2 *scratch,
+                                          const int *done, int *err, float2 *smem, int *failed)
+{
+	const fgk_plan4 *p = bg.p4;
+	const int L1 = (int)p->L1, L2 = (int)p->L2;
+	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
+	const int ls = (int)bg.ls2, nl = 1 << ls;
+	const int k1base = (int)(tk.a << ls);
+	const int nrow = min(nl, L1 - k1base);
+	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
+
+	/* every COLS tile of this item, bounded */
+	if (!tk_wait(done, (int)bg.ncols, err, failed))
+		return;
+
+	const float2 *Stile = scratch + bg.scratch_off + (uint64_t)tk.a * ((uint64_t)L2 << ls);
+	float *o = out_base + bg.out_off;
+	float2 *o2 = reinterpret_cast<float2 *>(o);
+	const float2 *q1 = (const float2 *)p->n1, *q2 = (const float2 *)p->n2;
+	auto ld = [&](int n2, int lane) { return __ldcg(Stile + (((uint32_t)n2 << ls) + (uint32_t)lane)); };
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		if (lane >= nrow)
+			return;
+		const int k2 = j + q * nbf;
+		const int k1 = k1base + lane;
+		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * (uint32_t)k2;
+		if (!inverse) {
+			if (!freq)
+				__stcs(o2 + m, v);
+			else if (m < ((L + 1) >> 1))
+				__stcs(o2 + 2 * m, v);
+			else
+				__stcs(o2 + 2 * (L - 1 - m) + 1, conjf2(v));
+		} else if (freq) {
+			const float2 r = cmul(v, cmul(__ldg(q1 + k1), __ldg(q2 + k2)));
+			__stcs(o + m, r.x);
+			__stcs(o + L + m, r.y);
+		} else {
+			__stcs(o2 + m, conjf2(v));
+		}
+	};
+	/* once the first stage has read the tile, drop its L2 lines without
+	 * writing them back */
+	auto discard = [&] {
+		const uintptr_t b0 = reinterpret_cast<uintptr_t>(Stile);
+		const uintptr_t b1 = b0 + ((uintptr_t)L2 << ls) * sizeof(float2);
+		for (uintptr_t a = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)tid * 128; a + 128 <= b1; a += (uintptr_t)T * 128)
+			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+	};
+	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
+	                        discard);
+}
+
+/* ---- three-level items (fgk_plan3): passes A, B, C ------------------- */
+/* A: 16 adjacent columns c = n2 L3 + n3, DFT_L1 over n1 straight from the
+ * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
+ * A[k1][c] (a warp's 16 lanes write one 128-byte segment). */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
+                                        float2 *scratch, int *done, float2 *smem)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L3 = (int)p->L3;
+	const uint32_t L23 = p->L2 * p->L3, L = (uint32_t)L1 * L23;
+	const int cbase = (int)(tk.a << 4);
+	const float inv3 = 1.0f / (float)L3;
+	const float *x = in_base + hg.in_off;
+	const float2 *x2 = reinterpret_cast<const float2 *>(x);
+	const float2 *ma = (const float2 *)p->ma, *mb = (const float2 *)p->mb, *mc = (const float2 *)p->mc;
+	const float2 *uhi = (const float2 *)p->uhi, *ulo = (const float2 *)p->ulo, *tq = (const float2 *)p->tq1;
+	const uint32_t ush = p->ushift, umask = (1u << ush) - 1;
+	float2 *A = scratch + hg.sa;
+	auto ld = [&](int n1, int lane) {
+		const uint32_t c = (uint32_t)(cbase + lane);
+		if (c >= L23)
+			return make_float2(0.f, 0.f);
+		const uint32_t n = (uint32_t)n1 * L23 + c;
+		if (!inverse) {
+			if (freq) {
+				const int n2 = tk_div((int)c, L3, inv3), n3 = (int)c - n2 * L3;
+				const float2 m = cmul(__ldg(ma + n1), cmul(__ldg(mb + n2), __ldg(mc + n3)));
+				return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), m);
+			}
+			return __ldcs(x2 + n);
+		}
+		if (freq)
+			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
+		return conjf2(__ldcs(x2 + n));
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const uint32_t c = (uint32_t)(cbase + lane);
+		if (c >= L23)
+			return;
+		const int n2 = tk_div((int)c, L3, inv3);
+		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
+		const float2 b = cmul(__ldg(uhi + (m >> ush)), __ldg(ulo + (m & umask)));
+		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : b;
+		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
+	};
+	tile_chain<false, Rows>(&p->c1, (const float2 *)p->tw1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+	tk_signal(done);
+}
+
+/* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
+ * n2 from A (32-byte segments), times w_L^{n3 (k1 + L1 k2)} =
+ * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
+                                        int *done_b, int *err, float2 *smem, int *failed)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const uint32_t L23 = (uint32_t)L2 * L3;
+	const int k1g = (int)(tk.a / hg.nb3);
+	const int k1b = k1g * 4, n3b = (int)(tk.a - (uint32_t)k1g * hg.nb3) * 4;
+	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo, *tq = (const float2 *)p->tq2;
+	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
+	const float2 *A = scratch + hg.sa;
+	float2 *B = scratch + hg.sb;
+	if (!tk_wait(done_a, (int)hg.na, err, failed))
+		return;
+	auto ld = [&](int n2, int lane) {
+		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
+		if (k1 >= L1 || n3 >= L3)
+			return make_float2(0.f, 0.f);
+		return __ldcg(A + (uint32_t)k1 * L23 + (uint32_t)n2 * L3 + n3);
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
+		if (k1 >= L1 || n3 >= L3)
+			return;
+		const uint32_t m = (uint32_t)n3 * ((uint32_t)k1 + (uint32_t)L1 * (uint32_t)j);
+		const float2 b = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
+		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
+	};
+	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+	tk_signal(done_b);
+}
+
+/* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from B (128-byte segments),
+ * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
+template <bool inverse, bool freq>
+__device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
+                                        const int *done_b, int *err, float2 *smem, int *failed)
+{
+	const fgk_plan3 *p = hg.p3;
+	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const uint32_t L = (uint32_t)L1 * L2 * L3;
+	const int k2 = (int)(tk.a / hg.nc1);
+	const int k1b = (int)(tk.a - (uint32_t)k2 * hg.nc1) * 16;
+	const float2 *B = scratch + hg.sb;
+	float *o = out_base + hg.out_off;
+	float2 *o2 = reinterpret_cast<float2 *>(o);
+	const float2 *oa = (const float2 *)p->oa, *ob = (const float2 *)p->ob, *oc = (const float2 *)p->oc;
+	if (!tk_wait(done_b, (int)hg.nb, err, failed))
+		return;
+	auto ld = [&](int n3, int lane) {
+		const int k1 = k1b + lane;
+		if (k1 >= L1)
+			return make_float2(0.f, 0.f);
+		return __ldcg(B + ((uint32_t)k2 * L3 + n3) * (uint32_t)L1 + k1);
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		const int k1 = k1b + lane;
+		if (k1 >= L1)
+			return;
+		const int k3 = j + q * nbf;
+		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * ((uint32_t)k2 + (uint32_t)L2 * k3);
+		if (!inverse) {
+			if (!freq)
+				__stcs(o2 + m, v);
+			else if (m < ((L + 1) >> 1))
+				__stcs(o2 + 2 * m, v);
+			else
+				__stcs(o2 + 2 * (L - 1 - m) + 1, conjf2(v));
+		} else if (freq) {
+			const float2 r = cmul(v, cmul(__ldg(oa + k1), cmul(__ldg(ob + k2), __ldg(oc + k3))));
+			__stcs(o + m, r.x);
+			__stcs(o + L + m, r.y);
+		} else {
+			__stcs(o2 + m, conjf2(v));
+		}
+	};
+	tile_chain<false, Rows>(&p->c3, (const float2 *)p->tw3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	                        (int)blockDim.x, true, ld, st, [] {});
+}
+
+/* One CTA: run tasks in claim order. Thread 0 claims the next task as the
+ * current one starts, so the claim's round trip overlaps the work. One
+ * instantiation per (direction, modulation): a batch has one of each. */
+template <bool inverse, bool freq>
+__global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
+    task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
+                const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
+                const fgk_huge *__restrict__ huges, int *counters, int *hcounters, float2 *scratch,
+                const float *in_base, float *out_base, int *err)
+{
+	extern __shared__ float2 smem[];
+	__shared__ uint32_t cur;
+	__shared__ fgk_task next_task;
+	__shared__ int failed;
+	uint32_t ahead = 0;
+	if (threadIdx.x == 0) {
+		cur = (uint32_t)atomicAdd(counters, 1);
+		if (cur < ntasks)
+			next_task = tasks[cur];
+	}
+	__syncthreads();
+	for (;;) {
+		const uint32_t c = cur;
+		if (c >= ntasks)
+			break;
+		const fgk_task tk = next_task;
+		if (threadIdx.x == 0)
+			ahead = (uint32_t)atomicAdd(counters, 1);
+		if (tk.kind == FGK_TASK_SMALL)
+			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem);
+		else if (tk.kind == FGK_TASK_COLS)
+			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem);
+		else if (tk.kind == FGK_TASK_ROWS)
+			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, smem,
+			                         &failed);
+		else if (tk.kind == FGK_TASK_PA)
+			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem);
+		else if (tk.kind == FGK_TASK_PB)
+			task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref, hcounters + 2 * tk.ref + 1, err,
+			                       smem, &failed);
+		else
+			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, smem,
+			                       &failed);
+		__syncthreads(); /* buffers are reused by the next task */
+		if (threadIdx.x == 0) {
+			cur = ahead;
+			if (ahead < ntasks)
+				next_task = tasks[ahead];
+		}
+		__syncthreads();
+	}
+}
+
+/* Launch of one instantiation (each lives in its own translation unit,
+ * fgk_tasks_<direction><modulation>.cu, so that the four compile in
+ * parallel); counters are already zeroed. */
+template <bool inverse, bool freq>
+int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans,
+                 const fgk_rg_item *items, const fgk_big *bigs, const fgk_huge *huges, int *counters,
+                 int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, cudaStream_t stream)
+{
+	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
+	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq>,
+	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess)
+		return (int)e;
+	task_kernel<inverse, freq><<<grid, TK_THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
+	                                                              hcounters, scratch, in_base, out_base, err);
+	return (int)cudaGetLastError();
+}
+
+} /* namespace fgk */
+
+#define FGKT_LAUNCH_ARGS                                                                                 \
+	uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans, const fgk_rg_item *items,     \
+	    const fgk_big *bigs, const fgk_huge *huges, int *counters, int *hcounters, float2 *scratch,              \
+	    const float *in_base, float *out_base, int *err, cudaStream_t stream
+#define FGKT_LAUNCH_PASS grid, tasks, ntasks, plans, items, bigs, huges, counters, hcounters, scratch, in_base, out_base, err, stream
