@@ -17,7 +17,7 @@ struct fftset_modulation {
 
 struct fs_impl;
 
-#define FS_MAX_VAR 8
+#define FS_MAX_VAR 16
 
 struct fftset_fft {
 	unsigned                        lfft;

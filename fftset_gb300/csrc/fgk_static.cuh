@@ -51,8 +51,17 @@ template <int MOD_, int L_, int T_, int G_, int TWG_, int MODE_, int... Rs> stru
 	static __host__ __device__ constexpr int ftw_size(int s) { return s == 0 ? 0 : (fr(s) - 1) * fns(s); }
 	static __host__ __device__ constexpr int itw_size(int s) { return s == 0 ? 0 : (ir(s) - 1) * ins(s); }
 	static __host__ __device__ constexpr int ftw_off(int s) { return s == 0 ? 0 : ftw_off(s - 1) + ftw_size(s - 1); }
-	static __host__ __device__ constexpr int itw_off(int s) { return s == 0 ? ftw_off(N) : itw_off(s - 1) + itw_size(s - 1); }
-	static constexpr int TW_TOTAL = itw_off(N);
+	/* a palindromic chain is its own reverse: the reversed stages read the
+	 * forward stages' twiddles (the host's table holds both; only the
+	 * forward half is staged) */
+	static __host__ __device__ constexpr bool pal(int s = 0) { return s >= N || (R[s] == R[N - 1 - s] && pal(s + 1)); }
+	static constexpr bool PAL = pal();
+	static __host__ __device__ constexpr int itw_off_full(int s)
+	{
+		return s == 0 ? ftw_off(N) : itw_off_full(s - 1) + itw_size(s - 1);
+	}
+	static __host__ __device__ constexpr int itw_off(int s) { return PAL ? ftw_off(s) : itw_off_full(s); }
+	static constexpr int TW_TOTAL = PAL ? ftw_off(N) : itw_off_full(N);
 	static constexpr int SLOTS = L + L / 16 + 1; /* padded exchange buffer */
 	static __host__ __device__ constexpr int slot(int i) { return i + (i >> 4); }
 };
@@ -174,7 +183,7 @@ __device__ __forceinline__ void inv_mid(int tid, int g, const Ex<C> &ex, const f
 template <class C, int S>
 __device__ __forceinline__ void stage_twiddles(float2 *tws, const float2 *__restrict__ gtw)
 {
-	if constexpr (S < 2 * C::N) {
+	if constexpr (S < (C::PAL ? C::N : 2 * C::N)) {
 		constexpr bool FW = S < C::N;
 		constexpr int ST = FW ? S : S - C::N;
 		if constexpr (ST > 0) {
