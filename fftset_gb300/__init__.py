@@ -69,6 +69,8 @@ _decl("fftset_fft_variants", C.c_int, [_vp])
 _decl("fftset_fft_variant", C.c_int, [_vp, C.c_int])
 _decl("fftset_fft_set_variant", C.c_int, [_vp, C.c_int, C.c_int])
 _decl("fftset_fft_autotune", C.c_int, [_vp, C.c_int, _u, C.POINTER(C.c_float)])
+_decl("fftset_tuning_save", C.c_int, [_P, C.c_char_p])
+_decl("fftset_tuning_load", C.c_int, [_P, C.c_char_p])
 
 OP_FORWARD, OP_INVERSE, OP_GET_KERNEL, OP_CONV, OP_CORR = range(5)
 
@@ -198,6 +200,22 @@ class FftSet:
         if e:
             cu = _lib.fftset_cuda_error(C.byref(self._s))
             raise FftsetError(f"{error_string(e)} (cuda error {cu})")
+
+    def save_tuning(self, path: str):
+        """fftset_tuning_save: the chosen kernels and task schedules of every
+        plan, for fftset_tuning_load in another process."""
+        rc = _lib.fftset_tuning_save(C.byref(self._s), os.fsencode(path))
+        if rc:
+            self.clear_error()
+            raise FftsetError(error_string(rc))
+
+    def load_tuning(self, path: str):
+        """fftset_tuning_load; raises FftsetError (UNSUPPORTED for a file from
+        another device model, INVALID for a malformed one)."""
+        rc = _lib.fftset_tuning_load(C.byref(self._s), os.fsencode(path))
+        if rc:
+            self.clear_error()
+            raise FftsetError(error_string(rc))
 
     def create_fft(self, modulation, complex_bins: int):
         h = _lib.fftset_create_fft(C.byref(self._s), _mod_ptr(modulation), complex_bins)

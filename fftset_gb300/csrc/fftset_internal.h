@@ -93,6 +93,9 @@ int  fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride,
                     unsigned count, cudaStream_t stream);
 struct fftset_ragged;
 void fsr_free(struct fftset_ragged *rb);
+/* applies a saved task-kernel schedule to a plan (fftset_ragged.c) */
+int  fsr_apply_schedule(struct fs_impl *fs, struct fftset_fft *f, const uint32_t *rad, uint32_t n, uint32_t tg,
+                        uint32_t ls1, uint32_t ls2);
 struct fs_impl *fs_impl_of(struct fftset *fc);
 /* grows staging slot `slot` to at least `bytes` (cudaMalloc) */
 int  fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);

@@ -578,6 +578,45 @@ static float fsr_time_size(struct fs_impl *fs, struct fftset_fft *f, int op, uns
 	return best;
 }
 
+/* Applies a saved per-size schedule (fftset_tuning_load): items up to a
+ * tile get the chain rad[0..n) (n == 0: the plan's own chain) with tg
+ * threads each; two-level items get 2^ls1 / 2^ls2 lanes per COLS / ROWS
+ * tile. The same checks as the autotuner's candidates. */
+int fsr_apply_schedule(struct fs_impl *fs, struct fftset_fft *f, const uint32_t *rad, uint32_t n, uint32_t tg,
+                       uint32_t ls1, uint32_t ls2)
+{
+	const uint32_t L = f->lfft;
+	int rc;
+	if (L > 65536)
+		return FFTSET_E_UNSUPPORTED;
+	if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
+		fgk_plan cand = f->rp;
+		void *dm = NULL;
+		uint32_t k, same = n == f->rp.fwd.nstages;
+		if (tg == 0 || tg > FSR_THREADS || (tg & 31))
+			return FFTSET_E_INVALID;
+		for (k = 0; same && k < n; k++)
+			same = rad[k] == f->rp.fwd.st[k].radix;
+		if (n && !same && (rc = fsr_candidate_plan(fs, f, rad, n, &cand, &dm)) != FFTSET_OK)
+			return rc;
+		if (f->rg_dmem)
+			cudaFree(f->rg_dmem);
+		f->rg_plan = cand;
+		f->rg_dmem = dm;
+		f->rg_tg = tg;
+		f->rg_tuned = 1;
+		return FFTSET_OK;
+	}
+	if ((rc = fs_ensure_fourstep(fs, f)) != FFTSET_OK)
+		return rc;
+	if (ls1 < 4 || ls2 < 4 || ls1 > fsr_lanes_log2(f->p4.L1, f->p4.L2) || ls2 > fsr_lanes_log2(f->p4.L2, f->p4.L1))
+		return FFTSET_E_INVALID;
+	f->rg_ls1 = ls1;
+	f->rg_ls2 = ls2;
+	f->rg_tuned = 1;
+	return FFTSET_OK;
+}
+
 int fftset_ragged_autotune(struct fftset_ragged *rb)
 {
 	struct fs_impl *fs;

@@ -218,6 +218,19 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
                                 size_t samples, const float *kernel_buf, unsigned kernel_length,
                                 unsigned block_length);
 
+/* No counterpart in the reference (its planner runs inside
+ * fftset_create_fft, src/fftset_vec.c:993-1152, and keeps nothing across
+ * processes). Persistent autotune results: fftset_tuning_save writes, for
+ * every plan of the fftset, the compiled kernel chosen per operation
+ * (fftset_fft_autotune / fftset_fft_set_variant) and the task schedule
+ * chosen by fftset_ragged_autotune, as text, with the device model it was
+ * measured on; fftset_tuning_load creates those plans in this fftset and
+ * applies the choices. Returns FFTSET_OK; FFTSET_E_UNSUPPORTED (nothing
+ * applied) for a file from another device model; FFTSET_E_INVALID for an
+ * unreadable or malformed file (records before the bad one stay applied). */
+int fftset_tuning_save(struct fftset *fs, const char *path);
+int fftset_tuning_load(struct fftset *fs, const char *path);
+
 /* No counterpart in the reference. A batched call (op FFTSET_OP_*, the
  * arguments of fftset_fft_*_batch) that allocates nothing, for callers that
  * must not call cudaMalloc while they run: a real-time audio callback with a
