@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libfftset_gb300.so")
@@ -156,6 +157,9 @@ class FftSet:
         if kernel_layout_width != 4:
             self.set_kernel_layout(kernel_layout_width)
         self._plans = {}
+        # ragged batches made from this fftset: fftset_destroy frees the
+        # plans they use, so they are destroyed first
+        self._ragged = weakref.WeakSet()
 
     @property
     def handle(self):
@@ -163,6 +167,8 @@ class FftSet:
 
     def close(self):
         if self._s.impl:
+            for r in list(getattr(self, "_ragged", ())):
+                r.close()
             _lib.fftset_destroy(C.byref(self._s))
             self._plans.clear()
 
@@ -366,6 +372,7 @@ class Ragged:
             owner.check()
             raise FftsetError("fftset_ragged_create failed")
         self.n = n
+        owner._ragged.add(self)
 
     @property
     def bytes(self) -> float:
@@ -398,8 +405,11 @@ class Ragged:
         return out
 
     def close(self):
+        """fftset_ragged_destroy (before its fftset's destroy: FftSet.close
+        calls this for every batch still open)."""
         if getattr(self, "h", None):
-            _lib.fftset_ragged_destroy(self.h)
+            if self.owner._s.impl:
+                _lib.fftset_ragged_destroy(self.h)
             self.h = None
 
     def __del__(self):

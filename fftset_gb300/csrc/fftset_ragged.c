@@ -661,11 +661,14 @@ int fftset_ragged_autotune(struct fftset_ragged *rb)
 			for (k = 0; k < nr[0]; k++)
 				rad[0][k] = f->rp.fwd.st[k].radix;
 			nc = 1;
-			if (nr[0] > 1) { /* reversed order: smallest radix first */
+			if (nr[0] > 1) { /* reversed order: smallest radix first (unless it is the same chain) */
+				uint32_t pal = 1;
 				nr[1] = nr[0];
-				for (k = 0; k < nr[0]; k++)
+				for (k = 0; k < nr[0]; k++) {
 					rad[1][k] = rad[0][nr[0] - 1 - k];
-				nc = 2;
+					pal &= rad[1][k] == rad[0][k];
+				}
+				nc = pal ? 1 : 2;
 			}
 			for (c = 0; c < nc; c++) {
 				fgk_plan cand;

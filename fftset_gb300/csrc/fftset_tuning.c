@@ -67,7 +67,12 @@ int fftset_tuning_save(struct fftset *fc, const char *path)
 			fprintf(fp, " %d", f->sel[op]);
 		fputc('\n', fp);
 		if (f->rg_tuned) {
-			uint32_t s, n = f->rg_dmem ? f->rg_plan.fwd.nstages : 0;
+			/* the chain only when it is not the plan's own */
+			uint32_t s, n = f->rg_plan.fwd.nstages, own = n == f->rp.fwd.nstages;
+			for (s = 0; own && s < n; s++)
+				own = f->rg_plan.fwd.st[s].radix == f->rp.fwd.st[s].radix;
+			if (!f->rg_dmem || own)
+				n = 0;
 			fprintf(fp, "ragged %d %u %u", mod, f->lfft, n);
 			for (s = 0; s < n; s++)
 				fprintf(fp, " %u", f->rg_plan.fwd.st[s].radix);

@@ -3,9 +3,11 @@
  * Every task is a tile of at most FGKT_POINTS points held in two padded
  * shared-memory buffers (ping-pong Stockham stages, one butterfly per thread
  * at a time, runtime radix; fgk_pingpong.cuh), so one CTA of 256 threads
- * needs 70 KB and three CTAs share an SM: while one loads its tile from HBM
- * the others compute, which is what keeps enough bytes in flight. Loads are
- * issued eight per thread before any is used.
+ * needs 70 KB; two CTAs share an SM, which leaves each thread 128 registers
+ * (no spills: at three CTAs the 80-register budget spilled to local memory,
+ * and the measured batches ran 5-17 % slower) and the SM about 110 KB of L1
+ * for the twiddle tables. Loads are issued eight per thread before any is
+ * used.
  *
  *   SMALL  n items of one size L <= FGKT_POINTS, whole transforms side
  *          by side (tg threads each), HBM in, HBM out.
@@ -51,7 +53,7 @@ namespace fgk {
 #define FGKT_THREADS 256 /* threads of a task CTA */
 #endif
 #ifndef FGKT_MIN_CTAS
-#define FGKT_MIN_CTAS 3 /* resident CTAs per SM the registers are budgeted for */
+#define FGKT_MIN_CTAS 2 /* resident CTAs per SM the registers are budgeted for */
 #endif
 constexpr int TK_THREADS = FGKT_THREADS;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */

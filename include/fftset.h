@@ -184,6 +184,8 @@ unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb);
  * the fastest on the size's plan (later batches of the same fftset reuse
  * it), then rebuilds rb's task list. */
 int      fftset_ragged_autotune(struct fftset_ragged *rb);
+/* Frees rb. A batch uses its fftset's plans, which fftset_destroy frees
+ * (like the reference's plans, fftset.h:49-52): destroy every batch first. */
 void     fftset_ragged_destroy(struct fftset_ragged *rb);
 
 /* Adjoint of fftset_fft_conv (the reference has only the forward,

@@ -115,3 +115,16 @@ def test_tuning_refuses_other_device_and_bad_files(fftset_lib, tmp_path):
         T.load_tuning(str(tmp_path / "missing.txt"))
     S.close()
     T.close()
+
+
+def test_ragged_closed_with_its_fftset(fftset_lib):
+    """Closing an FftSet first destroys the ragged batches still open on it
+    (their plans go with the fftset), so a batch collected afterwards is a
+    no-op rather than a use of freed memory."""
+    fs = fftset_lib
+    S = fs.FftSet()
+    rb = fs.Ragged(S, fs.COMPLEX, fs.OP_FORWARD, [64, 5120], [0, 128], [0, 128])
+    S.close()
+    assert rb.h is None
+    rb.close()
+    del rb
