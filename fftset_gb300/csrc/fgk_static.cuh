@@ -26,15 +26,34 @@
 
 namespace fgk {
 
-/* MODE: 0 in-place exchange buffer, direct HBM loads; 1 in-place with
- * inputs double-buffered by bulk copies (TMA); 2 ping-pong exchange buffers
- * (out-of-place stages, one barrier per stage, one butterfly at a time) */
+/* MODE (low two bits): 0 in-place exchange buffer, direct HBM loads; 1
+ * in-place with inputs double-buffered by bulk copies (TMA); 2 ping-pong
+ * exchange buffers (out-of-place stages, one barrier per stage, one
+ * butterfly at a time). MODE | 4 (direct-load modes only): group g hands
+ * butterfly j to thread (j - 32 g) mod T instead of thread j. Warps go to
+ * the SM's four schedulers by warp index mod 4, so when a stage has fewer
+ * butterflies than threads (radix 16 of 1536 bins: 96 for 128 threads) the
+ * idle warp is a different scheduler's in each group instead of always the
+ * last one's. */
+/* TWG_ (table flags): | 1 twiddles read from global memory (L1) instead of
+ * shared; | 2 radix >= 8 stages read the twiddles of p = 1, 2, 4, 8 only and
+ * form the others as products (fewer shared-memory reads, a few more
+ * multiplies); | 4 (ping-pong, FREQ_OFFSET_REAL) the modulation factors of
+ * the first and last stages from one table entry per butterfly times
+ * compile-time constants instead of one entry per point. */
 template <int MOD_, int L_, int T_, int G_, int TWG_, int MODE_, int... Rs> struct SCfg {
 	static constexpr int MOD = MOD_;
-	static constexpr bool TWG = TWG_ != 0; /* twiddles read from global memory (L1) instead of shared */
-	static constexpr int MODE = MODE_;
-	static constexpr bool TMA = MODE_ == 1;
-	static constexpr bool PP = MODE_ == 2;
+	static constexpr bool TWG = (TWG_ & 1) != 0;
+	static constexpr bool TWR = (TWG_ & 2) != 0;
+	static constexpr bool MODC = (TWG_ & 4) != 0;
+	static_assert(!(MODC && (MODE_ & 3) != 2), "constant modulation is a ping-pong form");
+	static constexpr int MODE = MODE_ & 3;
+	static constexpr bool TMA = MODE == 1;
+	static constexpr bool PP = MODE == 2;
+	static constexpr bool ROT = (MODE_ & 4) != 0;
+	static_assert(!(ROT && MODE == 1), "rotation is for the direct-load modes");
+	/* work index of thread t of group g (a bijection of 0..T-1) */
+	static __device__ __forceinline__ int wt(int t, int g) { return ROT ? (t + 32 * g) % T : t; }
 	static constexpr int L = L_;
 	static constexpr int T = T_;
 	static constexpr int G = G_;
@@ -80,6 +99,71 @@ __device__ __forceinline__ float2 ldcs2(const float2 *p) { return __ldcs(p); }
 __device__ __forceinline__ void stcs(float *p, float v) { __stcs(p, v); }
 __device__ __forceinline__ void stcs2(float2 *p, float2 v) { __stcs(p, v); }
 
+/* highest power of two <= p (p >= 1) */
+__host__ __device__ constexpr int hipow2(int p) { return p >= 16 ? 16 : p >= 8 ? 8 : p >= 4 ? 4 : p >= 2 ? 2 : 1; }
+
+/* Input twiddles of butterfly k of a stage (R, NS): v[p] *= w^{p k} for
+ * p = 1..R-1, the table holding entry (p-1, k) at tws[(p-1) NS + k] (shared)
+ * or tws[k (R-1) + p-1] (global, TWG). With TWR and R >= 8 only the entries
+ * of p = 1, 2, 4, 8 are read and w^{p k} = w^{h k} w^{(p-h) k} (h the
+ * highest power of two below p), at most three products deep. */
+template <class C, int R, int NS>
+__device__ __forceinline__ void twiddle_in(float2 (&v)[R], const float2 *tws, int k)
+{
+	auto entry = [&](int p) { return C::TWG ? __ldg(tws + k * (R - 1) + (p - 1)) : tws[(p - 1) * NS + k]; };
+	if constexpr (C::TWR && R >= 8) {
+		float2 w[R];
+#pragma unroll
+		for (int p = 1; p < R; p++)
+			w[p] = p == hipow2(p) ? entry(p) : cmul(w[hipow2(p)], w[p - hipow2(p)]);
+#pragma unroll
+		for (int p = 1; p < R; p++)
+			v[p] = cmul(v[p], w[p]);
+	} else {
+#pragma unroll
+		for (int p = 1; p < R; p++)
+			v[p] = cmul(v[p], entry(p));
+	}
+}
+
+/* cos and sin by their Taylor series (|x| <= pi/2), for compile-time
+ * constants only */
+__host__ __device__ constexpr double cx_sin(double x)
+{
+	double t = x, s = x;
+	for (int n = 1; n < 14; n++) {
+		t *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
+		s += t;
+	}
+	return s;
+}
+__host__ __device__ constexpr double cx_cos(double x)
+{
+	double t = 1.0, s = 1.0;
+	for (int n = 1; n < 14; n++) {
+		t *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
+		s += t;
+	}
+	return s;
+}
+
+/* e^{-j pi P / (2R)}: the ratio between the modulation factors of points
+ * i + P L/R and i (the factors are e^{-j pi i / (2L)}) */
+template <int R, int P> struct ModStep {
+	static constexpr double a = 3.14159265358979323846 * P / (2.0 * R);
+	static constexpr float re = (float)cx_cos(a);
+	static constexpr float im = (float)-cx_sin(a);
+};
+
+/* v[P..R-1] *= m e^{-j pi P / (2R)} */
+template <int R, int P = 0> __device__ __forceinline__ void mod_steps(float2 (&v)[R], float2 m)
+{
+	if constexpr (P < R) {
+		v[P] = cmul(v[P], P == 0 ? m : cmul(m, make_float2(ModStep<R, P>::re, ModStep<R, P>::im)));
+		mod_steps<R, P + 1>(v, m);
+	}
+}
+
 /* Tile of one stage: NB butterflies of radix R per thread. */
 template <class C, int R> struct Tile {
 	static constexpr int NBF = C::L / R;
@@ -109,12 +193,8 @@ template <class C, int R> struct Tile {
 		for (int b = 0; b < NB; b++) {
 			const int j = tid + b * C::T;
 			if (live(tid, b)) {
-				if constexpr (NS > 1) {
-					const int k = j % NS;
-#pragma unroll
-					for (int p = 1; p < R; p++)
-						v[b][p] = cmul(v[b][p], C::TWG ? __ldg(tws + k * (R - 1) + (p - 1)) : tws[(p - 1) * NS + k]);
-				}
+				if constexpr (NS > 1)
+					twiddle_in<C, R, NS>(v[b], tws, j % NS);
 				Radix<R>::run(v[b]);
 			}
 		}
@@ -440,7 +520,7 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel(const fgk_plan p,
 	__syncthreads();
 
 	const int g = threadIdx.x / C::T;
-	const int tid = threadIdx.x - g * C::T;
+	const int tid = C::wt((int)threadIdx.x - g * C::T, g);
 	const Ex<C> ex{exb + (size_t)g * C::SLOTS};
 	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {
 		const FirstLoad<C, OP, false> first{a.in + t * a.in_stride, mods};
@@ -538,16 +618,70 @@ __device__ __forceinline__ void pp_stage(int tid, const float2 *tws, Ld &&ld, St
 			for (int p = 0; p < R; p++)
 				v[p] = ld(j + p * NBF);
 			const int k = j % NS;
-			if constexpr (NS > 1) {
-#pragma unroll
-				for (int p = 1; p < R; p++)
-					v[p] = cmul(v[p], C::TWG ? __ldg(tws + k * (R - 1) + (p - 1)) : tws[(p - 1) * NS + k]);
-			}
+			if constexpr (NS > 1)
+				twiddle_in<C, R, NS>(v, tws, k);
 			Radix<R>::run(v);
 			const int base = (j - k) * R + k;
 #pragma unroll
 			for (int q = 0; q < R; q++)
 				st(base + q * NS, v[q]);
+		}
+	}
+}
+
+/* Constant-modulation forms (MODC, FREQ_OFFSET_REAL). The factor of point
+ * i is e^{-j pi i / (2L)}; the first stage's butterfly j reads the points
+ * j + p L/R and the last stage's butterfly j writes the points j + q L/R
+ * (its ns is L/R), so every factor is mods[j] e^{-j pi p / (2R)}: one table
+ * read per butterfly and compile-time constants. */
+template <class C, int OP, class St>
+__device__ __forceinline__ void pp_first_modc(int tid, const FirstLoad<C, OP, false> &first, const float2 *mods,
+                                              St &&st)
+{
+	constexpr int L = C::L, R = C::fr(0), NBF = L / R;
+	constexpr int NB = (NBF + C::T - 1) / C::T;
+	constexpr bool FULL = (NBF % C::T) == 0;
+#pragma unroll 2
+	for (int b = 0; b < NB; b++) {
+		const int j = tid + b * C::T;
+		if (FULL || j < NBF) {
+			float2 v[R];
+#pragma unroll
+			for (int p = 0; p < R; p++)
+				v[p] = make_float2(first.ld(j + p * NBF), -first.ld(L + j + p * NBF));
+			mod_steps<R>(v, mods[j]);
+			Radix<R>::run(v);
+#pragma unroll
+			for (int q = 0; q < R; q++)
+				st(j * R + q, v[q]);
+		}
+	}
+}
+
+template <class C, int R, int NS>
+__device__ __forceinline__ void pp_last_modc(int tid, const float2 *tws, const Ex<C> &src, float *y,
+                                             const float2 *mods)
+{
+	constexpr int L = C::L, NBF = L / R;
+	static_assert(NS == NBF, "the last stage's ns is L/R");
+	constexpr int NB = (NBF + C::T - 1) / C::T;
+	constexpr bool FULL = (NBF % C::T) == 0;
+#pragma unroll 2
+	for (int b = 0; b < NB; b++) {
+		const int j = tid + b * C::T;
+		if (FULL || j < NBF) {
+			float2 v[R];
+#pragma unroll
+			for (int p = 0; p < R; p++)
+				v[p] = src(j + p * NBF);
+			twiddle_in<C, R, NS>(v, tws, j);
+			Radix<R>::run(v);
+			mod_steps<R>(v, mods[j]);
+#pragma unroll
+			for (int q = 0; q < R; q++) {
+				stcs(y + j + q * NBF, v[q].x);
+				stcs(y + L + j + q * NBF, v[q].y);
+			}
 		}
 	}
 }
@@ -602,7 +736,10 @@ __device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float
 	};
 	const Ex<C> b0{buf0};
 	/* stage 0: HBM -> buffer 0 */
-	pp_stage<C, C::fr(0), 1>(tid, tws, first, [&](int i, float2 v) { b0.put(i, v); });
+	if constexpr (C::MODC && FREQ && OP != FGK_OP_INVERSE)
+		pp_first_modc<C, OP>(tid, first, mods, [&](int i, float2 v) { b0.put(i, v); });
+	else
+		pp_stage<C, C::fr(0), 1>(tid, tws, first, [&](int i, float2 v) { b0.put(i, v); });
 	gsync<C>(g);
 	pp_fwd<C, 1, N - 1>(tid, g, buf0, buf1, tws);
 	/* stage N-1 reads buffer (N-2)&1 */
@@ -619,12 +756,8 @@ __device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float
 #pragma unroll
 				for (int p = 0; p < R; p++)
 					v[p] = src(j + p * NBF);
-				if constexpr (NS > 1) {
-					const float2 *t = tws + C::ftw_off(N - 1);
-#pragma unroll
-					for (int p = 1; p < R; p++)
-						v[p] = cmul(v[p], C::TWG ? __ldg(t + j * (R - 1) + (p - 1)) : t[(p - 1) * NS + j]);
-				}
+				if constexpr (NS > 1)
+					twiddle_in<C, R, NS>(v, tws + C::ftw_off(N - 1), j);
 				Radix<R>::run(v);
 #pragma unroll
 				for (int q = 0; q < R; q++)
@@ -640,14 +773,19 @@ __device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float
 		constexpr int RL = C::ir(N - 1), NSL = C::ins(N - 1);
 		constexpr int RD = (2 * N - 3) & 1; /* reversed stage N-1 is global stage 2N-2 */
 		const Ex<C> last{RD ? buf1 : buf0};
-		pp_stage<C, RL, NSL>(tid, tws + C::itw_off(N - 1), last, out_final);
+		if constexpr (C::MODC && FREQ)
+			pp_last_modc<C, RL, NSL>(tid, tws + C::itw_off(N - 1), last, y, mods);
+		else
+			pp_stage<C, RL, NSL>(tid, tws + C::itw_off(N - 1), last, out_final);
 		/* the next transform's stage 0 writes buffer 0: if this stage read
 		 * it, every thread must be done first */
 		if constexpr (RD == 0)
 			gsync<C>(g);
 	} else {
 		constexpr int R = C::fr(N - 1), NS = C::fns(N - 1);
-		if constexpr (OP == FGK_OP_INVERSE) {
+		if constexpr (OP == FGK_OP_INVERSE && C::MODC && FREQ) {
+			pp_last_modc<C, R, NS>(tid, tws + C::ftw_off(N - 1), src, y, mods);
+		} else if constexpr (OP == FGK_OP_INVERSE) {
 			pp_stage<C, R, NS>(tid, tws + C::ftw_off(N - 1), src, out_final);
 		} else if constexpr (!FREQ) {
 			pp_stage<C, R, NS>(tid, tws + C::ftw_off(N - 1), src,
@@ -680,7 +818,7 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_pp(const fgk_plan
 	__syncthreads();
 
 	const int g = threadIdx.x / C::T;
-	const int tid = threadIdx.x - g * C::T;
+	const int tid = C::wt((int)threadIdx.x - g * C::T, g);
 	float2 *buf0 = exb + (size_t)(2 * g) * C::SLOTS;
 	float2 *buf1 = buf0 + C::SLOTS;
 	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {

@@ -298,10 +298,10 @@ __device__ __forceinline__ void tk_signal(int *ctr)
 /* n items of one size, tg threads each (group g = threadIdx / tg), each
  * group's first stage reading its item and its last stage writing its
  * output directly. */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *__restrict__ plans,
                                            const fgk_rg_item *__restrict__ items, const float *in_base,
-                                           float *out_base, float2 *smem)
+                                           float *out_base, float2 *smem, Pre &&pre)
 {
 	const fgk_plan *pl = plans + tk.ref;
 	const int L = (int)pl->L;
@@ -346,16 +346,16 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 		}
 	};
 	tile_chain<false, Pad>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
-	                       [] {});
+	                       pre);
 }
 
 /* COLS: columns n2base .. n2base + 2^ls1 - 1, DFTs of length L1 from the
  * input into the item's scratch, which is laid out by ROWS tiles: element
  * (k1, n2) at ((k1 >> ls2) L2 + n2) 2^ls2 + (k1 & (2^ls2 - 1)), so a ROWS
  * tile reads one contiguous block with its lanes fastest. */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, const float *in_base,
-                                          float2 *scratch, int *done, float2 *smem)
+                                          float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
@@ -398,15 +398,15 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 		       cmul(v, w));
 	};
 	tile_chain<true, Rows>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                       (int)blockDim.x, true, ld, st, [] {});
+	                       (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
 
 /* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
  * into X[k1 + L1 k2] */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, float *out_base, float2 *scratch,
-                                          const int *done, int *err, float2 *smem, int *failed)
+                                          const int *done, int *err, float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
@@ -455,16 +455,19 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
 	};
 	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
-	                        discard);
+	                        [&] {
+		                        discard();
+		                        pre();
+	                        });
 }
 
 /* ---- three-level items (fgk_plan3): passes A, B, C ------------------- */
 /* A: 16 adjacent columns c = n2 L3 + n3, DFT_L1 over n1 straight from the
  * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
  * A[k1][c] (a warp's 16 lanes write one 128-byte segment). */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
-                                        float2 *scratch, int *done, float2 *smem)
+                                        float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L3 = (int)p->L3;
@@ -505,16 +508,16 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
 		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
 	};
 	tile_chain<false, Rows>(&p->c1, (const float2 *)p->tw1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                        (int)blockDim.x, true, ld, st, [] {});
+	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
 
 /* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
  * n2 from A (32-byte segments), times w_L^{n3 (k1 + L1 k2)} =
  * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
-                                        int *done_b, int *err, float2 *smem, int *failed)
+                                        int *done_b, int *err, float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
@@ -543,15 +546,15 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
 	};
 	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                        (int)blockDim.x, true, ld, st, [] {});
+	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done_b);
 }
 
 /* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from B (128-byte segments),
  * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
-                                        const int *done_b, int *err, float2 *smem, int *failed)
+                                        const int *done_b, int *err, float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
@@ -592,7 +595,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 		}
 	};
 	tile_chain<false, Rows>(&p->c3, (const float2 *)p->tw3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                        (int)blockDim.x, true, ld, st, [] {});
+	                        (int)blockDim.x, true, ld, st, pre);
 }
 
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the
@@ -607,9 +610,25 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
-	__shared__ fgk_task next_task;
+	__shared__ __align__(16) fgk_task next_task;
 	__shared__ int failed;
 	uint32_t ahead = 0;
+	/* thread 0 copies the record of the task claimed ahead into next_task
+	 * (an asynchronous 16-byte copy) once the current task's first stage is
+	 * done: the claim has returned by then, every thread has read
+	 * next_task at the top of the loop, and the copy's round trip overlaps
+	 * the rest of the task */
+	bool copying = false;
+	auto pre = [&] {
+		if (threadIdx.x == 0 && !copying && ahead < ntasks) {
+			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+			                 (uint32_t)__cvta_generic_to_shared(&next_task)),
+			             "l"(tasks + ahead)
+			             : "memory");
+			asm volatile("cp.async.commit_group;" ::: "memory");
+			copying = true;
+		}
+	};
 	if (threadIdx.x == 0) {
 		cur = (uint32_t)atomicAdd(counters, 1);
 		if (cur < ntasks)
@@ -624,27 +643,39 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 		if (threadIdx.x == 0)
 			ahead = (uint32_t)atomicAdd(counters, 1);
 		if (tk.kind == FGK_TASK_SMALL)
-			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem);
+			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem, pre);
 		else if (tk.kind == FGK_TASK_COLS)
-			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem);
+			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_ROWS)
 			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, smem,
-			                         &failed);
+			                         &failed, pre);
 		else if (tk.kind == FGK_TASK_PA)
-			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem);
+			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_PB)
 			task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref, hcounters + 2 * tk.ref + 1, err,
-			                       smem, &failed);
+			                       smem, &failed, pre);
 		else
 			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, smem,
-			                       &failed);
-		__syncthreads(); /* buffers are reused by the next task */
+			                       &failed, pre);
 		if (threadIdx.x == 0) {
+			if (copying) {
+				asm volatile("cp.async.wait_all;" ::: "memory");
+				/* the next task's descriptor lines into L1 while the other
+				 * warps finish this one */
+				const fgk_task n = next_task;
+				const void *d = n.kind == FGK_TASK_SMALL ? (const void *)(plans + n.ref)
+				                : n.kind <= FGK_TASK_ROWS ? (const void *)(bigs + n.ref)
+				                                           : (const void *)(huges + n.ref);
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(d));
+				if (n.kind == FGK_TASK_SMALL)
+					asm volatile("prefetch.global.L1 [%0];" ::"l"(items + n.a));
+			} else if (ahead < ntasks) {
+				next_task = tasks[ahead]; /* a ROWS wait that gave up skipped the copy */
+			}
+			copying = false;
 			cur = ahead;
-			if (ahead < ntasks)
-				next_task = tasks[ahead];
 		}
-		__syncthreads();
+		__syncthreads(); /* buffers are reused by the next task */
 	}
 }
 
