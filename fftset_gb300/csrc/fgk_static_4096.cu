@@ -1,31 +1,40 @@
 /* Compile-time kernels for FREQ_OFFSET_REAL, 4096 bins (the batched
  * differentiable convolution workload): 16^3, 256 threads per transform.
- * SCfg<modulation, L, T, G, twiddles-from-global, mode, radices...> (mode 0
- * in place, 1 in place with bulk-copy input, 2 ping-pong). The first
- * variant that implements an op is its default: the order is the measured
- * one, fastest first (2048 and 16384 blocks on a GB300: V0 0.056 / 0.342 ms
- * for the convolution, V1 0.064 / 0.375, V3 0.070 / 0.479, V2 0.086 /
- * 0.549); the chain is a palindrome, so its twiddles are staged once. */
+ * SCfg<modulation, L, T, G, table flags, mode, radices...> (table flags
+ * | 2 radix-16 twiddles from the entries of p = 1, 2, 4, 8, | 4 modulation
+ * factors from one entry per butterfly and constants; mode 0 in place, 1 in
+ * place with bulk-copy input, 2 ping-pong). The first variant that
+ * implements an op is its default: the order is the measured one, fastest
+ * first (2048 blocks on a GB300, convolution / forward in ms: V0 0.0542 /
+ * 0.0444, V1 0.0553 / 0.0449, V2 0.0614, V3 0.0621, V4 0.0656 / 0.0518,
+ * V5 0.0660, V6 0.0861 / 0.0434); the chain is a palindrome, so its
+ * twiddles are staged once. */
 #include "fgk_static.cuh"
 
 namespace fgk {
-using V0 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 0, 0, 16, 16, 16>;
-using V1 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 0, 0, 16, 16, 16>;
-using V2 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 1, 1, 16, 16, 16>;
-using V3 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 0, 2, 16, 16, 16>;
+using V0 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 2, 0, 16, 16, 16>;
+using V1 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 0, 0, 16, 16, 16>;
+using V2 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 2, 0, 16, 16, 16>;
+using V3 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 0, 0, 16, 16, 16>;
+using V4 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 6, 2, 16, 16, 16>;
+using V5 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 0, 2, 16, 16, 16>;
+using V6 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 1, 1, 16, 16, 16>;
 
 int static_entries_4096(const StaticEntry **out)
 {
-	static StaticEntry t[4];
+	static StaticEntry t[7];
 	static bool init = false;
 	if (!init) {
 		t[0] = make_entry<V0, OPS_ALL>();
-		t[1] = make_entry<V1, OPS_CONV_CORR>();
-		t[2] = make_entry<V2, OPS_ALL>();
+		t[1] = make_entry<V1, OPS_ALL>();
+		t[2] = make_entry<V2, OPS_CONV_CORR>();
 		t[3] = make_entry<V3, OPS_CONV_CORR>();
+		t[4] = make_entry<V4, OPS_ALL>();
+		t[5] = make_entry<V5, OPS_CONV_CORR>();
+		t[6] = make_entry<V6, OPS_ALL>();
 		init = true;
 	}
 	*out = t;
-	return 4;
+	return 7;
 }
 } /* namespace fgk */
