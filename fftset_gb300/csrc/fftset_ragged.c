@@ -26,12 +26,15 @@
 #include "fftset_internal.h"
 #include "fgk.h"
 
-#define FSR_THREADS ((uint32_t)fgk_tasks_threads()) /* threads of a task CTA */
+/* threads of a narrow task CTA: per-size thread counts (tuned or not) stay
+ * within it, so they fit both CTA shapes */
+#define FSR_THREADS ((uint32_t)fgk_tasks_threads(0))
 
 struct fftset_ragged {
 	struct fs_impl *fs;
 	int             op;
 	int             modulation; /* FGK_MOD_* */
+	int             wide;       /* CTA shape: 1 when the list has three-level items */
 	unsigned        n;
 	fgk_task       *tasks_dev;
 	uint32_t        ntasks;
@@ -172,6 +175,8 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		order[i].bins = bins[i];
 		order[i].idx = i;
 		rb->bytes += 16.0 * bins[i];
+		if (bins[i] > 65536)
+			rb->wide = 1; /* three-level items measured faster on wide CTAs */
 	}
 	qsort(order, n, sizeof(*order), fsr_cmp);
 
@@ -188,7 +193,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
 			const fgk_plan *pl = f->rg_tuned && f->rg_dmem ? &f->rg_plan : &f->rp;
 			const uint32_t tg = f->rg_tuned ? f->rg_tg : fsr_item_threads(pl);
-			uint32_t G = FSR_THREADS / tg;
+			uint32_t G = (uint32_t)fgk_tasks_threads(rb->wide) / tg;
 			if (G * fsr_slots(L) > (uint32_t)fgk_tasks_slots())
 				G = (uint32_t)fgk_tasks_slots() / fsr_slots(L);
 			plans[nplans] = *pl;
@@ -262,7 +267,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	}
 	/* big items: COLS of item b, ROWS of item b - D */
 	if (nbig) {
-		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms);
+		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms, rb->wide);
 		const uint64_t avg = (total_cols + nbig - 1) / nbig;
 		uint32_t D = (uint32_t)((2 * grid + avg - 1) / avg) + 1, b, t;
 		for (b = 0; b < nbig + D; b++) {
@@ -368,7 +373,7 @@ static int fsr_record(struct fftset_ragged *rb, float *out, const float *in, cud
 	struct fs_impl *fs = rb->fs;
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
 	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, rb->op, rb->modulation, in, out,
-	                        fs->num_sms, fs->dev_flag, s);
+	                        fs->num_sms, rb->wide, fs->dev_flag, s);
 }
 
 int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)

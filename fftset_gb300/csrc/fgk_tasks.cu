@@ -1,13 +1,17 @@
 /* Host entry points of the ragged task kernel (fgk_tasks.cuh): its tile
  * geometry, and the launch, which zeroes the dependency counters and calls
- * the instantiation for the batch's direction and modulation
- * (fgk_tasks_{fc,ff,ic,if}.cu). */
+ * the instantiation for the batch's direction, modulation and CTA shape
+ * (fgk_tasks_{fc,ff,ic,if}[w].cu). */
 #include "fgk_tasks.cuh"
 
 extern "C" int fgk_launch_tasks_fc(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ff(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ic(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_if(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_fcw(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_ffw(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_icw(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_ifw(FGKT_LAUNCH_ARGS);
 
 extern "C" int fgk_tasks_points(void)
 {
@@ -19,21 +23,21 @@ extern "C" int fgk_tasks_slots(void)
 	return fgk::TK_SLOTS;
 }
 
-extern "C" int fgk_tasks_threads(void)
+extern "C" int fgk_tasks_threads(int wide)
 {
-	return FGKT_THREADS;
+	return wide ? fgk::TK_THREADS_WIDE : fgk::TK_THREADS_NARROW;
 }
 
-extern "C" int fgk_tasks_grid(int num_sms)
+extern "C" int fgk_tasks_grid(int num_sms, int wide)
 {
-	return FGKT_MIN_CTAS * num_sms;
+	return (wide ? fgk::TK_CTAS_WIDE : fgk::TK_CTAS_NARROW) * num_sms;
 }
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                                 const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev, float *scratch_dev,
                                 int op, int modulation, const float *in_base, float *out_base, int num_sms,
-                                int *err_flag, void *stream)
+                                int wide, int *err_flag, void *stream)
 {
 	const bool inv = op == FGK_OP_INVERSE, freq = modulation == FGK_MOD_FREQOFF;
 	cudaStream_t s = (cudaStream_t)stream;
@@ -43,13 +47,15 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig + 2 * (size_t)nhuge), s)) !=
 	    cudaSuccess)
 		return (int)e;
-	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms);
+	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms, wide);
 	if (grid > ntasks)
 		grid = ntasks;
 	int *hcounters = counters_dev + 1 + nbig;
 	float2 *scratch = reinterpret_cast<float2 *>(scratch_dev);
-	auto launch = inv ? (freq ? fgk_launch_tasks_if : fgk_launch_tasks_ic)
-	                  : (freq ? fgk_launch_tasks_ff : fgk_launch_tasks_fc);
+	auto launch = wide ? (inv ? (freq ? fgk_launch_tasks_ifw : fgk_launch_tasks_icw)
+	                          : (freq ? fgk_launch_tasks_ffw : fgk_launch_tasks_fcw))
+	                   : (inv ? (freq ? fgk_launch_tasks_if : fgk_launch_tasks_ic)
+	                          : (freq ? fgk_launch_tasks_ff : fgk_launch_tasks_fc));
 	return launch(grid, tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, huges_dev, counters_dev, hcounters, scratch,
 	              in_base, out_base, err_flag, s);
 }

@@ -2,12 +2,9 @@
  *
  * Every task is a tile of at most FGKT_POINTS points held in two padded
  * shared-memory buffers (ping-pong Stockham stages, one butterfly per thread
- * at a time, runtime radix; fgk_pingpong.cuh), so one CTA of 256 threads
- * needs 70 KB; two CTAs share an SM, which leaves each thread 128 registers
- * (no spills: at three CTAs the 80-register budget spilled to local memory,
- * and the measured batches ran 5-17 % slower) and the SM about 110 KB of L1
- * for the twiddle tables. Loads are issued eight per thread before any is
- * used.
+ * at a time, runtime radix; fgk_pingpong.cuh), 70 KB per CTA; a CTA has 128
+ * threads (three CTAs per SM) or 256 (two per SM), see TK_THREADS_NARROW.
+ * Loads are issued eight per thread before any is used.
  *
  *   SMALL  n items of one size L <= FGKT_POINTS, whole transforms side
  *          by side (tg threads each), HBM in, HBM out.
@@ -49,13 +46,15 @@ namespace fgk {
 #ifndef FGKT_POINTS
 #define FGKT_POINTS 4096 /* points of a tile */
 #endif
-#ifndef FGKT_THREADS
-#define FGKT_THREADS 256 /* threads of a task CTA */
-#endif
-#ifndef FGKT_MIN_CTAS
-#define FGKT_MIN_CTAS 2 /* resident CTAs per SM the registers are budgeted for */
-#endif
-constexpr int TK_THREADS = FGKT_THREADS;
+/* Two CTA shapes, chosen per task list: narrow, 128 threads and three CTAs
+ * per SM (three tiles in flight per SM, 168 registers a thread), for lists
+ * of items up to 65536 bins (the ragged mix: 1.998 against 2.106 ms for the
+ * 20000-item batch); wide, 256 threads and two CTAs per SM (128 registers),
+ * for lists with three-level items (the 15,728,640-bin transform: 0.737
+ * against 0.786 ms). Both shapes fit the 128-register budget with no
+ * spills; at three CTAs of 256 threads (80 registers) the kernel spilled. */
+constexpr int TK_THREADS_NARROW = 128, TK_CTAS_NARROW = 3;
+constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 2;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
 constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
 constexpr uint32_t TK_SPIN_LIMIT = 1u << 22;                         /* x 256 ns: about a second */
@@ -618,8 +617,8 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the
  * current one starts, so the claim's round trip overlaps the work. One
  * instantiation per (direction, modulation): a batch has one of each. */
-template <bool inverse, bool freq>
-__global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
+template <bool inverse, bool freq, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
                 const fgk_huge *__restrict__ huges, int *counters, int *hcounters, float2 *scratch,
@@ -697,19 +696,19 @@ __global__ void __launch_bounds__(TK_THREADS, FGKT_MIN_CTAS)
 }
 
 /* Launch of one instantiation (each lives in its own translation unit,
- * fgk_tasks_<direction><modulation>.cu, so that the four compile in
+ * fgk_tasks_<direction><modulation>[w].cu, so that the eight compile in
  * parallel); counters are already zeroed. */
-template <bool inverse, bool freq>
+template <bool inverse, bool freq, int THREADS, int MINB>
 int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans,
                  const fgk_rg_item *items, const fgk_big *bigs, const fgk_huge *huges, int *counters,
                  int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, cudaStream_t stream)
 {
 	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
-	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq>,
+	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq, THREADS, MINB>,
 	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess)
 		return (int)e;
-	task_kernel<inverse, freq><<<grid, TK_THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
+	task_kernel<inverse, freq, THREADS, MINB><<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
 	                                                              hcounters, scratch, in_base, out_base, err);
 	return (int)cudaGetLastError();
 }

@@ -1,0 +1,7 @@
+/* The ragged task kernel (inverse, COMPLEX), wide CTAs; fgk_tasks.cuh. */
+#include "fgk_tasks.cuh"
+
+extern "C" int fgk_launch_tasks_icw(FGKT_LAUNCH_ARGS)
+{
+	return fgk::launch_tasks<true, false, fgk::TK_THREADS_WIDE, fgk::TK_CTAS_WIDE>(FGKT_LAUNCH_PASS);
+}
