@@ -1,19 +1,23 @@
 /* Compile-time kernels for FREQ_OFFSET_REAL, 4096 bins (the batched
  * differentiable convolution workload): 16^3, 256 threads per transform.
  * SCfg<modulation, L, T, G, table flags, mode, radices...> (table flags
- * | 2 radix-16 twiddles from the entries of p = 1, 2, 4, 8, | 4 modulation
- * factors from one entry per butterfly and constants; mode 0 in place, 1 in
- * place with bulk-copy input, 2 ping-pong). The first variant that
- * implements an op is its default: the order is the measured one, fastest
- * first (2048 blocks on a GB300, convolution / forward in ms: V0 0.0542 /
- * 0.0444, V1 0.0553 / 0.0449, V2 0.0614, V3 0.0621, V4 0.0656 / 0.0518,
- * V5 0.0660, V6 0.0861 / 0.0434); the chain is a palindrome, so its
- * twiddles are staged once. */
+ * | 1 twiddles through L1, | 2 radix-16 twiddles from the entries of
+ * p = 1, 2, 4, 8, | 4 modulation factors from one entry per butterfly and
+ * constants; mode 0 in place, 1 in place with bulk-copy input, 2 ping-pong).
+ * The first variant that implements an op is its default: the order is the
+ * measured one, fastest first (GB300, convolution at 2048 / 16384 blocks in
+ * ms: V0 0.0553 / 0.341, V1 0.0587 / 0.345, V2 0.0619 / 0.370, V3 0.0624 /
+ * 0.371, V4 0.0658 / 0.458, V5 0.0676 / 0.474, V6 0.0848 / 0.542; forward at
+ * 16384 blocks: V0 0.245, V1 0.250, V6 0.289; inverse: V1 0.215, V0 0.221).
+ * Unlike the 1536-bin kernels, fewer twiddle reads do not pay here: at
+ * 4096 bins a thread runs one radix-16 butterfly per stage with all 256
+ * threads busy, and the extra multiplies lengthen it. The chain is a
+ * palindrome, so its twiddles are staged once. */
 #include "fgk_static.cuh"
 
 namespace fgk {
-using V0 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 2, 0, 16, 16, 16>;
-using V1 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 0, 0, 16, 16, 16>;
+using V0 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 0, 0, 16, 16, 16>;
+using V1 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 2, 0, 16, 16, 16>;
 using V2 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 2, 0, 16, 16, 16>;
 using V3 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 0, 0, 16, 16, 16>;
 using V4 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 6, 2, 16, 16, 16>;
