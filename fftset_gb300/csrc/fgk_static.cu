@@ -6,6 +6,8 @@ namespace fgk {
 int static_entries_1536(const StaticEntry **out);
 int static_entries_4096(const StaticEntry **out);
 int static_entries_1024(const StaticEntry **out);
+int static_entries_c1536(const StaticEntry **out);
+int static_entries_c4096(const StaticEntry **out);
 
 static int variants(uint32_t mod, uint32_t L, const StaticEntry **out)
 {
@@ -17,6 +19,10 @@ static int variants(uint32_t mod, uint32_t L, const StaticEntry **out)
 		n = static_entries_4096(&e);
 	else if (mod == FGK_MOD_COMPLEX && L == 1024)
 		n = static_entries_1024(&e);
+	else if (mod == FGK_MOD_COMPLEX && L == 1536)
+		n = static_entries_c1536(&e);
+	else if (mod == FGK_MOD_COMPLEX && L == 4096)
+		n = static_entries_c4096(&e);
 	*out = e;
 	return n;
 }

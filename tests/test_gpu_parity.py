@@ -272,7 +272,7 @@ def test_other_simd_layouts(fftset_lib, golden_layouts, vw):
         S.close()
 
 
-STATIC = [(1, 1536), (1, 4096), (0, 1024)]
+STATIC = [(1, 1536), (1, 4096), (0, 1024), (0, 1536), (0, 4096)]
 
 
 @pytest.mark.parametrize("mod,L", STATIC)
