@@ -14,8 +14,10 @@
 
 #ifdef __CUDACC__
 #define FGK_HD __host__ __device__ __forceinline__
+#define FGK_CX __host__ __device__ constexpr
 #else
 #define FGK_HD inline
+#define FGK_CX constexpr
 #include <cmath>
 struct float2 { float x, y; };
 static inline float2 make_float2(float a, float b) { float2 r; r.x = a; r.y = b; return r; }
@@ -57,6 +59,60 @@ FGK_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 /* a * (-j) */
 FGK_HD float2 mul_mj(float2 a) { return make_float2(a.y, -a.x); }
 FGK_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+/* ---- lean tables --------------------------------------------------------
+ * Helpers for kernels that read fewer table entries and multiply instead. */
+
+/* highest power of two <= p, for 1 <= p < 32 */
+FGK_CX int hipow2(int p) { return p >= 16 ? 16 : p >= 8 ? 8 : p >= 4 ? 4 : p >= 2 ? 2 : 1; }
+
+/* w[p] = w^{p k} for p = 1..R-1, where entry(p) reads w^{p k} from a table:
+ * only the entries of p = 1, 2, 4, 8 are read and the others formed as
+ * w^{h k} w^{(p-h) k}, h = hipow2(p), at most three products deep. */
+template <int R, class Entry> FGK_HD void twiddle_powers(float2 (&w)[R], Entry &&entry)
+{
+#pragma unroll
+	for (int p = 1; p < R; p++)
+		w[p] = p == hipow2(p) ? entry(p) : cmul(w[hipow2(p)], w[p - hipow2(p)]);
+}
+
+/* sin and cos by their Taylor series for |x| <= pi/2, for compile-time
+ * constants */
+FGK_CX double cx_sin(double x)
+{
+	double t = x, s = x;
+	for (int n = 1; n < 14; n++) {
+		t *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
+		s += t;
+	}
+	return s;
+}
+FGK_CX double cx_cos(double x)
+{
+	double t = 1.0, s = 1.0;
+	for (int n = 1; n < 14; n++) {
+		t *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
+		s += t;
+	}
+	return s;
+}
+
+/* e^{-j pi P / (2R)}: the ratio between the FREQ_OFFSET_REAL modulation
+ * factors e^{-j pi i / (2L)} of points i + P L/R and i */
+template <int R, int P> struct ModStep {
+	static constexpr double a = 3.14159265358979323846 * P / (2.0 * R);
+	static constexpr float re = (float)cx_cos(a);
+	static constexpr float im = (float)-cx_sin(a);
+};
+
+/* v[P..R-1] *= m e^{-j pi P / (2R)} */
+template <int R, int P = 0> FGK_HD void mod_steps(float2 (&v)[R], float2 m)
+{
+	if constexpr (P < R) {
+		v[P] = cmul(v[P], P == 0 ? m : cmul(m, make_float2(ModStep<R, P>::re, ModStep<R, P>::im)));
+		mod_steps<R, P + 1>(v, m);
+	}
+}
 
 /* exact decimal expansions of the constants named */
 #define FGK_SQRT1_2 0.70710678118654752440f  /* cos(pi/4) */
@@ -209,7 +265,7 @@ template <> struct Radix<16> { static FGK_HD void run(float2 *v) { dft16(v); } }
 /* Good-Thomas prime-factor composite for N = A*B, gcd(A,B) = 1:
  * input  n = (B n1 + A n2) mod N,
  * output k = (B (B^-1 mod A) k1 + A (A^-1 mod B) k2) mod N. */
-constexpr int fgk_inv_mod(int a, int m, int t = 1)
+FGK_CX int fgk_inv_mod(int a, int m, int t = 1)
 {
 	return ((a * t) % m == 1) ? t : fgk_inv_mod(a, m, t + 1);
 }

@@ -99,23 +99,17 @@ __device__ __forceinline__ float2 ldcs2(const float2 *p) { return __ldcs(p); }
 __device__ __forceinline__ void stcs(float *p, float v) { __stcs(p, v); }
 __device__ __forceinline__ void stcs2(float2 *p, float2 v) { __stcs(p, v); }
 
-/* highest power of two <= p (p >= 1) */
-__host__ __device__ constexpr int hipow2(int p) { return p >= 16 ? 16 : p >= 8 ? 8 : p >= 4 ? 4 : p >= 2 ? 2 : 1; }
-
 /* Input twiddles of butterfly k of a stage (R, NS): v[p] *= w^{p k} for
  * p = 1..R-1, the table holding entry (p-1, k) at tws[(p-1) NS + k] (shared)
  * or tws[k (R-1) + p-1] (global, TWG). With TWR and R >= 8 only the entries
- * of p = 1, 2, 4, 8 are read and w^{p k} = w^{h k} w^{(p-h) k} (h the
- * highest power of two below p), at most three products deep. */
+ * of p = 1, 2, 4, 8 are read (twiddle_powers, fgk_codelets.cuh). */
 template <class C, int R, int NS>
 __device__ __forceinline__ void twiddle_in(float2 (&v)[R], const float2 *tws, int k)
 {
 	auto entry = [&](int p) { return C::TWG ? __ldg(tws + k * (R - 1) + (p - 1)) : tws[(p - 1) * NS + k]; };
 	if constexpr (C::TWR && R >= 8) {
 		float2 w[R];
-#pragma unroll
-		for (int p = 1; p < R; p++)
-			w[p] = p == hipow2(p) ? entry(p) : cmul(w[hipow2(p)], w[p - hipow2(p)]);
+		twiddle_powers<R>(w, entry);
 #pragma unroll
 		for (int p = 1; p < R; p++)
 			v[p] = cmul(v[p], w[p]);
@@ -123,44 +117,6 @@ __device__ __forceinline__ void twiddle_in(float2 (&v)[R], const float2 *tws, in
 #pragma unroll
 		for (int p = 1; p < R; p++)
 			v[p] = cmul(v[p], entry(p));
-	}
-}
-
-/* cos and sin by their Taylor series (|x| <= pi/2), for compile-time
- * constants only */
-__host__ __device__ constexpr double cx_sin(double x)
-{
-	double t = x, s = x;
-	for (int n = 1; n < 14; n++) {
-		t *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
-		s += t;
-	}
-	return s;
-}
-__host__ __device__ constexpr double cx_cos(double x)
-{
-	double t = 1.0, s = 1.0;
-	for (int n = 1; n < 14; n++) {
-		t *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
-		s += t;
-	}
-	return s;
-}
-
-/* e^{-j pi P / (2R)}: the ratio between the modulation factors of points
- * i + P L/R and i (the factors are e^{-j pi i / (2L)}) */
-template <int R, int P> struct ModStep {
-	static constexpr double a = 3.14159265358979323846 * P / (2.0 * R);
-	static constexpr float re = (float)cx_cos(a);
-	static constexpr float im = (float)-cx_sin(a);
-};
-
-/* v[P..R-1] *= m e^{-j pi P / (2R)} */
-template <int R, int P = 0> __device__ __forceinline__ void mod_steps(float2 (&v)[R], float2 m)
-{
-	if constexpr (P < R) {
-		v[P] = cmul(v[P], P == 0 ? m : cmul(m, make_float2(ModStep<R, P>::re, ModStep<R, P>::im)));
-		mod_steps<R, P + 1>(v, m);
 	}
 }
 

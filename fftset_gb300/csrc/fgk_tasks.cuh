@@ -88,19 +88,14 @@ struct Rows {
 
 /* v[p] *= w^{p k} (p = 1..R-1) from the butterfly's row t of the stage's
  * twiddle table (t[p-1] = w^{p k}). Radix 8 and above read the entries of
- * p = 1, 2, 4, 8 only and form the others as w^{p k} = w^{h k} w^{(p-h) k}
- * (h the highest power of two below p, at most three products deep):
- * 4 instead of 15 table reads for radix 16, which go through an L1 shared
- * with many sizes' tables. */
+ * p = 1, 2, 4, 8 only and form the others as products (twiddle_powers,
+ * fgk_codelets.cuh): 4 instead of 15 table reads for radix 16, which go
+ * through an L1 shared with many sizes' tables. */
 template <int R> __device__ __forceinline__ void tk_twiddle(float2 (&v)[R], const float2 *__restrict__ t)
 {
 	if constexpr (R >= 8) {
 		float2 w[R];
-#pragma unroll
-		for (int p = 1; p < R; p++) {
-			const int h = p >= 8 ? 8 : p >= 4 ? 4 : p >= 2 ? 2 : 1;
-			w[p] = p == h ? __ldg(t + p - 1) : cmul(w[h], w[p - h]);
-		}
+		twiddle_powers<R>(w, [&](int p) { return __ldg(t + p - 1); });
 #pragma unroll
 		for (int p = 1; p < R; p++)
 			v[p] = cmul(v[p], w[p]);
