@@ -7,7 +7,7 @@
  * Pass 2 (rows): for each k1, DFT_L2 over n2 of y[k1 L2 + n2], result
  *   X[k1 + L1 k2].
  * Each HBM array is read once and written once per pass (two passes per
- * transform, SURVEY's four-step schedule). A CTA owns NL transforms of one
+ * transform). A CTA owns NL transforms of one
  * pass (NL adjacent columns, or NL adjacent rows) and keeps them lane-
  * interleaved in shared memory (element i of lane l at slot(i NL + l)), so
  * its HBM accesses are NL-element contiguous segments.
