@@ -275,12 +275,32 @@ void oracle_plan_destroy(struct oracle_plan *p)
 	free(p);
 }
 
+/* The composite codelets' internal twiddles w_r^m = e^{-j 2 pi m / r}
+ * (r = 6, 8, 16, m < r), each computed once in FP64 and rounded to FP32:
+ * the values a per-butterfly cos/sin would give, without calling them for
+ * every butterfly. Filled by oracle_plan_create. */
+static float or_cw[17][16][2];
+static pthread_once_t or_cw_once = PTHREAD_ONCE_INIT;
+
+static void or_cw_init(void)
+{
+	static const unsigned rs[3] = {6, 8, 16};
+	unsigned i, m;
+	for (i = 0; i < 3; i++)
+		for (m = 0; m < rs[i]; m++) {
+			double ang = -2.0 * M_PI * (double)m / (double)rs[i];
+			or_cw[rs[i]][m][0] = (float)cos(ang);
+			or_cw[rs[i]][m][1] = (float)sin(ang);
+		}
+}
+
 struct oracle_plan *oracle_plan_create(int modulation, unsigned L, unsigned build_vw)
 {
 	struct oracle_plan *p;
 	unsigned chain[OR_MAX_CHAIN], n, i, len, s;
 	if (L < 2)
 		return NULL;
+	pthread_once(&or_cw_once, or_cw_init);
 	p = (struct oracle_plan *)calloc(1, sizeof(*p));
 	if (!p)
 		return NULL;
@@ -338,111 +358,101 @@ unsigned oracle_plan_lanes(const struct oracle_plan *p) { return p->V; }
 #define OR_C5D 0.58778525229247312917f /* sin(pi/5) */
 #define OR_R2  0.70710678118654752440f
 
-static inline void or_dft2(float *re, float *im)
-{
-	float ar = re[0] + re[1], ai = im[0] + im[1];
-	float br = re[0] - re[1], bi = im[0] - im[1];
-	re[0] = ar; im[0] = ai; re[1] = br; im[1] = bi;
-}
+typedef float or_v4 __attribute__((vector_size(16)));
 
-static inline void or_dft3(float *re, float *im)
-{
-	float sr = re[1] + re[2], si = im[1] + im[2];
-	float dr = re[1] - re[2], di = im[1] - im[2];
-	float mr = re[0] - 0.5f * sr, mi = im[0] - 0.5f * si;
-	re[0] += sr; im[0] += si;
-	re[1] = mr + OR_C3 * di; im[1] = mi - OR_C3 * dr;
-	re[2] = mr - OR_C3 * di; im[2] = mi + OR_C3 * dr;
-}
-
-static inline void or_dft4(float *re, float *im)
-{
-	float ar = re[0] + re[2], ai = im[0] + im[2];
-	float br = re[0] - re[2], bi = im[0] - im[2];
-	float cr = re[1] + re[3], ci = im[1] + im[3];
-	float dr = re[1] - re[3], di = im[1] - im[3];
-	re[0] = ar + cr; im[0] = ai + ci;
-	re[2] = ar - cr; im[2] = ai - ci;
-	re[1] = br + di; im[1] = bi - dr;
-	re[3] = br - di; im[3] = bi + dr;
-}
-
-static inline void or_dft5(float *re, float *im)
-{
-	float s1r = re[1] + re[4], s1i = im[1] + im[4];
-	float d1r = re[1] - re[4], d1i = im[1] - im[4];
-	float s2r = re[2] + re[3], s2i = im[2] + im[3];
-	float d2r = re[2] - re[3], d2i = im[2] - im[3];
-	float a1r = re[0] + OR_C5A * s1r - OR_C5C * s2r;
-	float a1i = im[0] + OR_C5A * s1i - OR_C5C * s2i;
-	float a2r = re[0] - OR_C5C * s1r + OR_C5A * s2r;
-	float a2i = im[0] - OR_C5C * s1i + OR_C5A * s2i;
-	float b1r = OR_C5B * d1i + OR_C5D * d2i;
-	float b1i = OR_C5B * d1r + OR_C5D * d2r;
-	float b2r = OR_C5D * d1i - OR_C5B * d2i;
-	float b2i = OR_C5D * d1r - OR_C5B * d2r;
-	re[0] += s1r + s2r; im[0] += s1i + s2i;
-	re[1] = a1r + b1r; im[1] = a1i - b1i;
-	re[4] = a1r - b1r; im[4] = a1i + b1i;
-	re[2] = a2r + b2r; im[2] = a2i - b2i;
-	re[3] = a2r - b2r; im[3] = a2i + b2i;
-}
-
-static void or_dft_small(unsigned r, float *re, float *im);
-
-/* r = a*b: X[b*k1 + k2] = sum_p1 w_a^{p1 k1} w_r^{p1 k2} sum_p2 x[p1 + a p2] w_b^{p2 k2} */
-static void or_dft_composite(unsigned a, unsigned b, float *re, float *im)
-{
-	float tr[16], ti[16], ur[16], ui[16];
-	unsigned p1, p2, k1, k2, r = a * b;
-	for (p1 = 0; p1 < a; p1++) {
-		float cr[16], ci[16];
-		for (p2 = 0; p2 < b; p2++) {
-			cr[p2] = re[p1 + a * p2];
-			ci[p2] = im[p1 + a * p2];
-		}
-		or_dft_small(b, cr, ci);
-		for (k2 = 0; k2 < b; k2++) {
-			double ang = -2.0 * M_PI * (double)(p1 * k2) / (double)r;
-			float wr = (float)cos(ang), wi = (float)sin(ang);
-			tr[p1 * b + k2] = cr[k2] * wr - ci[k2] * wi;
-			ti[p1 * b + k2] = cr[k2] * wi + ci[k2] * wr;
-		}
-	}
-	for (k2 = 0; k2 < b; k2++) {
-		for (p1 = 0; p1 < a; p1++) {
-			ur[p1] = tr[p1 * b + k2];
-			ui[p1] = ti[p1 * b + k2];
-		}
-		or_dft_small(a, ur, ui);
-		for (k1 = 0; k1 < a; k1++) {
-			re[b * k1 + k2] = ur[k1];
-			im[b * k1 + k2] = ui[k1];
-		}
-	}
-}
-
-static void or_dft_small(unsigned r, float *re, float *im)
-{
-	switch (r) {
-	case 2: or_dft2(re, im); break;
-	case 3: or_dft3(re, im); break;
-	case 4: or_dft4(re, im); break;
-	case 5: or_dft5(re, im); break;
-	case 6: or_dft_composite(2, 3, re, im); break;
-	case 8: or_dft_composite(2, 4, re, im); break;
-	case 16: or_dft_composite(4, 4, re, im); break;
-	default: break;
-	}
-}
+#define OR_T float
+#define OR_SFX
+#include "fftset_oracle_codelets.h"
+#undef OR_T
+#undef OR_SFX
+#define OR_T or_v4
+#define OR_SFX _v4
+#include "fftset_oracle_codelets.h"
+#undef OR_T
+#undef OR_SFX
 
 /* ------------------------------------------------------------------------
  * Passes over the lane layout. x points at slot 0; slot s real lane l is
  * x[2V s + l], imaginary x[2V s + V + l]. */
+static inline or_v4 or_ld4(const float *p)
+{
+	or_v4 v;
+	memcpy(&v, p, sizeof v);
+	return v;
+}
+
+static inline void or_st4(float *p, or_v4 v) { memcpy(p, &v, sizeof v); }
+
+/* Four lanes at a time (V a multiple of 4): the same operations per lane as
+ * the one-lane loops below. */
+static void or_pass_dif_v4(const struct or_pass *ps, unsigned V, unsigned nblk, float *x)
+{
+	unsigned r = ps->radix, m = ps->m, b, j, p, l;
+	or_v4 re[16], im[16];
+	for (b = 0; b < nblk; b++) {
+		float *blk = x + (size_t)b * r * m * 2 * V;
+		for (j = 0; j < m; j++) {
+			const float *tw = ps->tw ? ps->tw + 2 * (r - 1) * j : NULL;
+			for (l = 0; l < V; l += 4) {
+				for (p = 0; p < r; p++) {
+					re[p] = or_ld4(blk + 2 * V * (j + p * m) + l);
+					im[p] = or_ld4(blk + 2 * V * (j + p * m) + V + l);
+				}
+				or_dft_small_v4(r, re, im);
+				for (p = 0; p < r; p++) {
+					or_v4 orr = re[p], oi = im[p];
+					if (tw && p) {
+						float wr = tw[2 * (p - 1)], wi = tw[2 * (p - 1) + 1];
+						orr = re[p] * wr - im[p] * wi;
+						oi = re[p] * wi + im[p] * wr;
+					}
+					or_st4(blk + 2 * V * (j + p * m) + l, orr);
+					or_st4(blk + 2 * V * (j + p * m) + V + l, oi);
+				}
+			}
+		}
+	}
+}
+
+static void or_pass_dit_v4(const struct or_pass *ps, unsigned V, unsigned nblk, float *x)
+{
+	unsigned r = ps->radix, m = ps->m, b, j, p, l;
+	or_v4 re[16], im[16];
+	for (b = 0; b < nblk; b++) {
+		float *blk = x + (size_t)b * r * m * 2 * V;
+		for (j = 0; j < m; j++) {
+			const float *tw = ps->tw ? ps->tw + 2 * (r - 1) * j : NULL;
+			for (l = 0; l < V; l += 4) {
+				for (p = 0; p < r; p++) {
+					or_v4 ir = or_ld4(blk + 2 * V * (j + p * m) + l);
+					or_v4 ii = or_ld4(blk + 2 * V * (j + p * m) + V + l);
+					if (tw && p) {
+						float wr = tw[2 * (p - 1)], wi = tw[2 * (p - 1) + 1];
+						re[p] = ir * wr - ii * wi;
+						im[p] = ir * wi + ii * wr;
+					} else {
+						re[p] = ir;
+						im[p] = ii;
+					}
+				}
+				or_dft_small_v4(r, re, im);
+				for (p = 0; p < r; p++) {
+					or_st4(blk + 2 * V * (j + p * m) + l, re[p]);
+					or_st4(blk + 2 * V * (j + p * m) + V + l, im[p]);
+				}
+			}
+		}
+	}
+}
+
 static void or_pass_dif(const struct or_pass *ps, unsigned V, unsigned nblk, float *x)
 {
 	unsigned r = ps->radix, m = ps->m, b, j, p, l;
 	float re[16], im[16];
+	if (V % 4 == 0) {
+		or_pass_dif_v4(ps, V, nblk, x);
+		return;
+	}
 	for (b = 0; b < nblk; b++) {
 		float *blk = x + (size_t)b * r * m * 2 * V;
 		for (j = 0; j < m; j++) {
@@ -472,6 +482,10 @@ static void or_pass_dit(const struct or_pass *ps, unsigned V, unsigned nblk, flo
 {
 	unsigned r = ps->radix, m = ps->m, b, j, p, l;
 	float re[16], im[16];
+	if (V % 4 == 0) {
+		or_pass_dit_v4(ps, V, nblk, x);
+		return;
+	}
 	for (b = 0; b < nblk; b++) {
 		float *blk = x + (size_t)b * r * m * 2 * V;
 		for (j = 0; j < m; j++) {
