@@ -20,7 +20,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["fgk_resident.cu", "fgk_static.cu", "fgk_static_1536.cu", "fgk_static_4096.cu", "fgk_static_1024.cu", "fgk_static_complex.cu", "fgk_fourstep.cu", "fgk_tasks.cu", "fgk_tasks_fc.cu", "fgk_tasks_ff.cu", "fgk_tasks_ic.cu", "fgk_tasks_if.cu", "fgk_tasks_fcw.cu", "fgk_tasks_ffw.cu", "fgk_tasks_icw.cu", "fgk_tasks_ifw.cu", "fgk_fixed_scratch.cu", "fgk_adjoint.cu", "fgk_ola.cu"]
-C_SOURCES = ["fftset_host.c", "fftset_layout.c", "fgk_plan.c", "fftset_ragged.c", "fftset_adjoint.c", "fftset_ola.c", "fftset_tuning.c"]
+C_SOURCES = ["fftset_alloc.c", "fftset_host.c", "fftset_layout.c", "fgk_plan.c", "fftset_ragged.c", "fftset_adjoint.c", "fftset_ola.c", "fftset_tuning.c"]
 HEADERS = ["fgk.h", "fgk_codelets.cuh", "fftset_layout.h", "fgk_static.cuh", "fftset_internal.h", "fgk_pingpong.cuh", "fgk_tasks.cuh"]
 
 
@@ -60,7 +60,7 @@ def build(verbose: bool = False) -> str:
     stamp = os.path.join(OUT, "link.stamp")
     key = ",".join(sorted(objs))
     if not (os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == key):
-        cmd = [NVCC, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart", "-lpthread", "-lm",
+        cmd = [NVCC, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart", "-lpthread", "-lm", "-ldl",
                "-Xlinker", "-rpath=" + os.path.join(CUDA, "lib64")]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

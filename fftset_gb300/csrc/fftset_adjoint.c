@@ -127,6 +127,7 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 		in_stride = nf;
 	}
 
+	FS_RANGE_PUSH("fftset_fft_conv_adjoint_batch");
 	pthread_mutex_lock(&fs->lock); /* the adjoint's scratch slot */
 	if (grad_input) {
 		rc = fs_launch(fft, FGK_OP_CORR, grad_input, grad_output, kernel_buf, count, go_stride, gi_stride);
@@ -144,5 +145,6 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 	}
 done:
 	pthread_mutex_unlock(&fs->lock);
+	FS_RANGE_POP();
 	return rc;
 }

@@ -42,12 +42,14 @@ struct fs_impl *fs_impl_of(struct fftset *fc)
 	return fs_of(fc);
 }
 
+/* The first error is kept until fftset_clear_error; calls on several
+ * threads may latch at once, so the slot is claimed with a compare-and-swap. */
 int fs_latch(struct fs_impl *fs, int code, int cuda_err)
 {
-	if (fs && code && !fs->err) {
-		fs->err = code;
-		fs->cuda_err = cuda_err;
-	}
+	int zero = 0;
+	if (fs && code &&
+	    __atomic_compare_exchange_n(&fs->err, &zero, code, 0, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE))
+		__atomic_store_n(&fs->cuda_err, cuda_err, __ATOMIC_RELEASE);
 	return code;
 }
 
@@ -84,10 +86,17 @@ int fftset_init(struct fftset *fc)
 		free(fs);
 		return -1;
 	}
-	if (pthread_mutex_init(&fs->lock, NULL) != 0) {
-		cudaStreamDestroy(fs->own_stream);
-		free(fs);
-		return -1;
+	{
+		pthread_mutexattr_t ma;
+		int bad = pthread_mutexattr_init(&ma) != 0;
+		bad = bad || pthread_mutexattr_settype(&ma, PTHREAD_MUTEX_RECURSIVE) != 0 ||
+		      pthread_mutex_init(&fs->lock, &ma) != 0;
+		pthread_mutexattr_destroy(&ma);
+		if (bad) {
+			cudaStreamDestroy(fs->own_stream);
+			free(fs);
+			return -1;
+		}
 	}
 	if (cudaHostAlloc((void **)&fs->host_flag, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
 	    cudaHostGetDevicePointer((void **)&fs->dev_flag, fs->host_flag, 0) != cudaSuccess) {
@@ -119,6 +128,7 @@ int fftset_init(struct fftset *fc)
 		}
 	}
 	fs->stream = fs->own_stream;
+	fs->spin_limit = 1u << 22; /* about a second */
 	fs->blocking = 1;
 	fs->layout_vw = 4;
 	fs->device = dev;
@@ -138,7 +148,8 @@ void fftset_destroy(struct fftset *fc)
 	cudaStreamSynchronize(fs->stream);
 	for (p = fs->first; p != NULL; p = n) {
 		n = p->next;
-		fsr_free(p->tasks);
+		for (i = 0; i < FS_TASK_LISTS; i++)
+			fsr_free(p->tl[i].rb);
 		cudaFree(p->rg_dmem);
 		cudaFree(p->dmem);
 		cudaFree(p->dmem4);
@@ -563,10 +574,19 @@ const struct fftset_fft *fftset_create_fft(struct fftset *fc, const struct fftse
 	return fs_create_plan(fs, modulation, complex_bins);
 }
 
+/* why the calling thread's last fs_create_plan returned NULL */
+static __thread int fs_plan_why;
+
+int fs_plan_error(void)
+{
+	return fs_plan_why;
+}
+
 struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modulation *modulation, unsigned complex_bins)
 {
 	struct fftset_fft *p, **ipos;
 	int rc;
+	fs_plan_why = FFTSET_E_INVALID;
 	if (modulation != FFTSET_MODULATION_COMPLEX && modulation != FFTSET_MODULATION_FREQ_OFFSET_REAL) {
 		fs_latch(fs, FFTSET_E_INVALID, 0);
 		return NULL;
@@ -583,6 +603,7 @@ struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modula
 	}
 	p = (struct fftset_fft *)calloc(1, sizeof(*p));
 	if (p == NULL) {
+		fs_plan_why = FFTSET_E_NOMEM;
 		fs_latch(fs, FFTSET_E_NOMEM, 0);
 		return NULL;
 	}
@@ -591,6 +612,7 @@ struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modula
 	p->fs = fs;
 	rc = fs_build_resident(fs, p);
 	if (rc) {
+		fs_plan_why = rc;
 		fs_latch(fs, rc, 0);
 		free(p);
 		return NULL;
@@ -655,13 +677,12 @@ int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
 	return FFTSET_OK;
 }
 
-/* A kernel whose bounded wait gave up wrote 1 to the mapped flag. */
+/* A kernel whose bounded wait gave up wrote 1 to the mapped flag; the
+ * thread that takes it latches the timeout. */
 int fs_check_flag(struct fs_impl *fs)
 {
-	if (*(volatile int *)fs->host_flag) {
-		*(volatile int *)fs->host_flag = 0;
+	if (__atomic_load_n(fs->host_flag, __ATOMIC_ACQUIRE) && __atomic_exchange_n(fs->host_flag, 0, __ATOMIC_ACQ_REL))
 		return fs_latch(fs, FFTSET_E_TIMEOUT, 0);
-	}
 	return FFTSET_OK;
 }
 
@@ -705,27 +726,40 @@ static int fs_launch_variant(const struct fftset_fft *f, int v, int op, float *o
 	return fs_launch_variant_ex(f, v, op, out, in, kern, count, in_stride, out_stride, stream, 0);
 }
 
-int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
-                     unsigned count, size_t in_stride, size_t out_stride)
+/* Plans beyond the shared-memory limit share state between calls (their
+ * cached task lists, the work buffer of staging slot 3, tables built on
+ * demand): calls on them hold the fftset's lock from lookup to launch, so
+ * that concurrent calls on several threads never launch on a list or a
+ * buffer another thread is replacing. */
+static int fs_launch_fourstep(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
+                              unsigned count, size_t in_stride, size_t out_stride)
 {
-	if (f->fourstep && (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE)) {
+	struct fs_impl *fs = f->fs;
+	const size_t nf = 2 * (size_t)f->lfft;
+	int rc = -FFTSET_E_UNSUPPORTED;
+	pthread_mutex_lock(&fs->lock);
+	if (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE)
 		/* tile tasks (fgk_tasks.cuh): two- or three-level split */
-		const int rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, f->fs->stream);
-		if (rc != -FFTSET_E_UNSUPPORTED)
-			return rc;
-	}
-	if (f->fourstep) {
+		rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, fs->stream);
+	if (rc == -FFTSET_E_UNSUPPORTED) {
 		/* two passes through a work buffer of 2L floats per transform (the
 		 * library's own scratch: work_buf of the reference API may be host
 		 * memory or too small for batches) */
-		struct fs_impl *fs = f->fs;
-		const size_t nf = 2 * (size_t)f->lfft;
-		int rc;
 		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0)
-			return -rc;
-		return fgk_launch_fourstep(&f->p4, op, out, in, kern, f->kidx4, (int)f->lanes, (float *)fs->stage[3],
-		                           count, in_stride ? in_stride : nf, out_stride ? out_stride : nf, nf, fs->stream);
+			rc = -rc;
+		else
+			rc = fgk_launch_fourstep(&f->p4, op, out, in, kern, f->kidx4, (int)f->lanes, (float *)fs->stage[3],
+			                         count, in_stride ? in_stride : nf, out_stride ? out_stride : nf, nf, fs->stream);
 	}
+	pthread_mutex_unlock(&fs->lock);
+	return rc;
+}
+
+int fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern,
+                     unsigned count, size_t in_stride, size_t out_stride)
+{
+	if (f->fourstep)
+		return fs_launch_fourstep(f, op, out, in, kern, count, in_stride, out_stride);
 	int v = count >= FS_STATIC_MIN_COUNT ? f->sel[op] : -1;
 	return fs_launch_variant(f, v, op, out, in, kern, count, in_stride, out_stride, f->fs->stream);
 }
@@ -943,49 +977,73 @@ done:
 void fftset_fft_forward(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf, float *work_buf)
 {
 	(void)work_buf;
+	FS_RANGE_PUSH("fftset_fft_forward");
 	fs_exec(first_pass, FGK_OP_FORWARD, output_buf, 0, input_buf, 0, NULL, 1);
+	FS_RANGE_POP();
 }
 
 void fftset_fft_inverse(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf, float *work_buf)
 {
 	(void)work_buf;
+	FS_RANGE_PUSH("fftset_fft_inverse");
 	fs_exec(first_pass, FGK_OP_INVERSE, output_buf, 0, input_buf, 0, NULL, 1);
+	FS_RANGE_POP();
 }
 
 void fftset_fft_conv_get_kernel(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf)
 {
+	FS_RANGE_PUSH("fftset_fft_conv_get_kernel");
 	fs_exec(first_pass, FGK_OP_KERNEL, output_buf, 0, input_buf, 0, NULL, 1);
+	FS_RANGE_POP();
 }
 
 void fftset_fft_conv(const struct fftset_fft *first_pass, float *output_buf, const float *input_buf,
                      const float *kernel_buf, float *work_buf)
 {
 	(void)work_buf;
+	FS_RANGE_PUSH("fftset_fft_conv");
 	fs_exec(first_pass, FGK_OP_CONV, output_buf, 0, input_buf, 0, kernel_buf, 1);
+	FS_RANGE_POP();
 }
 
 int fftset_fft_forward_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
                              const float *input_buf, size_t in_stride, unsigned count)
 {
-	return fs_exec(fft, FGK_OP_FORWARD, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	int rc;
+	FS_RANGE_PUSH("fftset_fft_forward_batch");
+	rc = fs_exec(fft, FGK_OP_FORWARD, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	FS_RANGE_POP();
+	return rc;
 }
 
 int fftset_fft_inverse_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
                              const float *input_buf, size_t in_stride, unsigned count)
 {
-	return fs_exec(fft, FGK_OP_INVERSE, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	int rc;
+	FS_RANGE_PUSH("fftset_fft_inverse_batch");
+	rc = fs_exec(fft, FGK_OP_INVERSE, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	FS_RANGE_POP();
+	return rc;
 }
 
 int fftset_fft_conv_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
                           const float *input_buf, size_t in_stride, const float *kernel_buf, unsigned count)
 {
-	return fs_exec(fft, FGK_OP_CONV, output_buf, out_stride, input_buf, in_stride, kernel_buf, count);
+	int rc;
+	FS_RANGE_PUSH("fftset_fft_conv_batch");
+	rc = fs_exec(fft, FGK_OP_CONV, output_buf, out_stride, input_buf, in_stride, kernel_buf, count);
+	FS_RANGE_POP();
+	return rc;
 }
 
 int fftset_fft_conv_get_kernel_batch(const struct fftset_fft *fft, float *output_buf, size_t out_stride,
                                      const float *input_buf, size_t in_stride, unsigned count)
 {
-	return fs_exec(fft, FGK_OP_KERNEL, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	int rc;
+	FS_RANGE_PUSH("fftset_fft_conv_get_kernel_batch");
+	rc = fs_exec(fft, FGK_OP_KERNEL, output_buf, out_stride, input_buf, in_stride, NULL, count);
+	FS_RANGE_POP();
+	return rc;
 }
 
 /* ------------------------------------------------------------------------
@@ -1025,7 +1083,7 @@ int fftset_last_error(const struct fftset *fc)
 	if (!fs)
 		return FFTSET_E_INVALID;
 	fs_check_flag(fs); /* picks up kernel reports of non-blocking calls once they finished */
-	return fs->err;
+	return __atomic_load_n(&fs->err, __ATOMIC_ACQUIRE);
 }
 
 int fftset_clear_error(struct fftset *fc)
@@ -1034,9 +1092,8 @@ int fftset_clear_error(struct fftset *fc)
 	int e;
 	if (!fs)
 		return FFTSET_E_INVALID;
-	e = fs->err;
-	fs->err = 0;
-	fs->cuda_err = 0;
+	e = __atomic_exchange_n(&fs->err, 0, __ATOMIC_ACQ_REL);
+	__atomic_store_n(&fs->cuda_err, 0, __ATOMIC_RELEASE);
 	return e;
 }
 
@@ -1078,6 +1135,15 @@ void *fftset_own_stream(const struct fftset *fc)
 {
 	struct fs_impl *fs = fs_of(fc);
 	return fs ? (void *)fs->own_stream : NULL;
+}
+
+int fftset__test_set_spin_limit(struct fftset *fc, unsigned polls)
+{
+	struct fs_impl *fs = fs_of(fc);
+	if (!fs || polls == 0)
+		return FFTSET_E_INVALID;
+	fs->spin_limit = polls;
+	return FFTSET_OK;
 }
 
 int fftset_set_blocking(struct fftset *fc, int blocking)

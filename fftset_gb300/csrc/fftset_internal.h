@@ -10,14 +10,22 @@
 #include "fftset.h"
 #include "fgk.h"
 
+/* NVTX ranges (header-only NVTX 3; inert unless a profiler is attached)
+ * around every public call, named after the call */
+#include <nvtx3/nvToolsExt.h>
+#define FS_RANGE_PUSH(name) nvtxRangePushA(name)
+#define FS_RANGE_POP()      nvtxRangePop()
+
 struct fftset_modulation {
 	int         freq_offset_real;
 	const char *name;
 };
 
 struct fs_impl;
+struct fftset_ragged;
 
 #define FS_MAX_VAR 16
+#define FS_TASK_LISTS 4 /* cached task lists per plan (shapes of the plain calls) */
 
 struct fftset_fft {
 	unsigned                        lfft;
@@ -37,7 +45,17 @@ struct fftset_fft {
 	const int32_t                  *kidx4; /* kernel-layout table in dmem4 */
 	fgk_plan3                       p3;    /* three-level plan (when dmem3 != NULL) */
 	void                           *dmem3; /* its device tables */
-	struct fftset_ragged           *tasks; /* cached task list of the plain calls (fftset_ragged.c) */
+	/* task lists of the plain calls of this plan (fftset_ragged.c), one per
+	 * (count, strides) shape seen, least recently used replaced first; the
+	 * direction is a launch argument, so a list serves both. Read and
+	 * written with fs->lock held. */
+	struct fs_tasklist {
+		struct fftset_ragged *rb;
+		unsigned              count;
+		size_t                in_stride, out_stride;
+		uint64_t              used;
+	} tl[FS_TASK_LISTS];
+	uint64_t                        tl_clock;
 	/* task-kernel schedule picked by fftset_ragged_autotune (rg_tuned):
 	 * whole items run rg_plan's chain (its tables in rg_dmem, NULL for the
 	 * default chain) with rg_tg threads each; two-level items use rg_ls1 /
@@ -46,8 +64,6 @@ struct fftset_fft {
 	fgk_plan                        rg_plan;
 	void                           *rg_dmem;
 	uint32_t                        rg_tg, rg_ls1, rg_ls2;
-	unsigned                        tasks_count;
-	size_t                          tasks_in_stride, tasks_out_stride;
 	void                           *dmem;  /* one device block for all tables */
 };
 
@@ -65,8 +81,14 @@ struct fs_impl {
 	unsigned           max_smem;
 	int                num_sms;
 	struct fftset_fft *first;
+	/* recursive: held around everything that touches state shared by the
+	 * execution calls of this fftset (staging buffers, the task lists and
+	 * on-demand tables of plans beyond the shared-memory limit), so that
+	 * those calls are thread-safe like the reference's (README.md:38);
+	 * resident-size calls share nothing and do not take it */
 	pthread_mutex_t    lock;
 	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
+	uint32_t           spin_limit; /* polls of a task kernel's bounded waits (fgk_launch_tasks) */
 	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
@@ -86,22 +108,57 @@ int  fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f);
 int  fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f);
 /* find-or-create a plan (fftset_create_fft without the public wrapper) */
 struct fftset_fft *fs_create_plan(struct fs_impl *fs, const struct fftset_modulation *modulation, unsigned bins);
+/* FFTSET_E_* code of the calling thread's last fs_create_plan that returned NULL */
+int  fs_plan_error(void);
 /* forward / inverse of `count` device blocks of a four-step plan as one task
  * launch (fftset_ragged.c); returns 0, a negative FFTSET_E_* code or a
- * positive cudaError_t; FFTSET_E_UNSUPPORTED when the size has no tile split */
+ * positive cudaError_t; FFTSET_E_UNSUPPORTED when the size has no tile split.
+ * Called with fs->lock held. */
 int  fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
                     unsigned count, cudaStream_t stream);
-struct fftset_ragged;
 void fsr_free(struct fftset_ragged *rb);
 /* applies a saved task-kernel schedule to a plan (fftset_ragged.c) */
 int  fsr_apply_schedule(struct fs_impl *fs, struct fftset_fft *f, const uint32_t *rad, uint32_t n, uint32_t tg,
                         uint32_t ls1, uint32_t ls2);
 struct fs_impl *fs_impl_of(struct fftset *fc);
-/* grows staging slot `slot` to at least `bytes` (cudaMalloc) */
+/* grows staging slot `slot` to at least `bytes` (cudaMalloc); called with
+ * fs->lock held */
 int  fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes);
 /* runs op on `count` device-resident blocks on the fftset's stream;
- * returns 0, a negative FFTSET_E_* code or a positive cudaError_t */
+ * returns 0, a negative FFTSET_E_* code or a positive cudaError_t. Takes
+ * fs->lock itself for plans beyond the shared-memory limit. */
 int  fs_launch(const struct fftset_fft *f, int op, float *out, const float *in, const float *kern, unsigned count,
                size_t in_stride, size_t out_stride);
+
+
+/* Allocation wrappers (fftset_alloc.c): the host layer's allocations are
+ * counted, and a test can make one of them fail. */
+void       *fs_malloc(size_t n);
+void       *fs_calloc(size_t n, size_t m);
+void        fs_free(void *p);
+cudaError_t fs_cuda_malloc(void **p, size_t n);
+cudaError_t fs_cuda_free(void *p);
+cudaError_t fs_cuda_host_alloc(void **p, size_t n, unsigned flags);
+cudaError_t fs_cuda_free_host(void *p);
+/* Test hooks, exported but not part of the public header: the nth host or
+ * device allocation from now fails (0: none; returns the previous setting),
+ * and the numbers of host and device allocations still held. */
+long fftset__test_fail_allocation(long nth);
+void fftset__test_live_allocations(long *host, long *device);
+/* Test hooks of the bounded waits: the polls of the task kernel's waits
+ * (launches made afterwards), and a ragged batch without its tasks of one
+ * kind (the tasks that wait on them then time out). */
+int  fftset__test_set_spin_limit(struct fftset *fc, unsigned polls);
+int  fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind);
+#if !defined(FS_ALLOC_IMPL) && !defined(__cplusplus)
+#include <stdlib.h>
+#define malloc(n)                 fs_malloc(n)
+#define calloc(n, m)              fs_calloc((n), (m))
+#define free(p)                   fs_free(p)
+#define cudaMalloc(p, n)          fs_cuda_malloc((void **)(p), (n))
+#define cudaFree(p)               fs_cuda_free(p)
+#define cudaHostAlloc(p, n, f)    fs_cuda_host_alloc((void **)(p), (n), (f))
+#define cudaFreeHost(p)           fs_cuda_free_host(p)
+#endif
 
 #endif

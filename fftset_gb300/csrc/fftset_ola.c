@@ -46,6 +46,7 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
 		return fs_latch(fs, FFTSET_E_INVALID, 0);
 	bytes = nblocks * nf * sizeof(float);
 
+	FS_RANGE_PUSH("fftset_fft_conv_overlap_add");
 	pthread_mutex_lock(&fs->lock); /* staging slots 0 and 1 */
 	if ((rc = fs_stage_reserve(fs, 0, bytes)) != 0 || (rc = fs_stage_reserve(fs, 1, bytes)) != 0)
 		goto done;
@@ -73,5 +74,6 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
 	}
 done:
 	pthread_mutex_unlock(&fs->lock);
+	FS_RANGE_POP();
 	return rc;
 }

@@ -130,6 +130,9 @@ void fftset_ragged_destroy(struct fftset_ragged *rb)
 	fsr_free(rb);
 }
 
+/* why the calling thread's last fsr_create returned NULL (FFTSET_E_*) */
+static __thread int fsr_why;
+
 static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_modulation *modulation, int op,
                                         unsigned n, const unsigned *bins, const size_t *in_offsets,
                                         const size_t *out_offsets)
@@ -147,6 +150,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	cudaError_t e;
 	int rc = FFTSET_E_NOMEM;
 
+	fsr_why = FFTSET_E_INVALID;
 	if (!fs)
 		return NULL;
 	if (n == 0 || !bins || !in_offsets || !out_offsets || (op != FFTSET_OP_FORWARD && op != FFTSET_OP_INVERSE)) {
@@ -187,7 +191,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		for (j = i; j < n && order[j].bins == L; j++)
 			;
 		if (!f) {
-			rc = FFTSET_E_INVALID;
+			rc = fs_plan_error();
 			goto fail;
 		}
 		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
@@ -346,6 +350,7 @@ cuda_fail:
 	cudaGetLastError();
 	rc = e == cudaErrorMemoryAllocation ? FFTSET_E_NOMEM : FFTSET_E_CUDA;
 fail:
+	fsr_why = rc;
 	fs_latch(fs, rc, 0);
 	free(order);
 	free(plans);
@@ -362,32 +367,90 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
                                            const size_t *out_offsets)
 {
 	struct fs_impl *fs = fs_impl_of(fc);
+	struct fftset_ragged *rb;
 	if (!fs)
 		return NULL;
-	return fsr_create(fs, modulation, op, n, bins, in_offsets, out_offsets);
+	/* plans and their on-demand tables are shared with the execution calls */
+	pthread_mutex_lock(&fs->lock);
+	rb = fsr_create(fs, modulation, op, n, bins, in_offsets, out_offsets);
+	pthread_mutex_unlock(&fs->lock);
+	return rb;
 }
 
-/* the launch sequence, on `s` */
-static int fsr_record(struct fftset_ragged *rb, float *out, const float *in, cudaStream_t s)
+/* the launch sequence of direction `op`, on `s` (a task list does not
+ * depend on the direction) */
+static int fsr_record(struct fftset_ragged *rb, int op, float *out, const float *in, cudaStream_t s)
 {
 	struct fs_impl *fs = rb->fs;
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
-	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, rb->op, rb->modulation, in, out,
-	                        fs->num_sms, rb->wide, fs->dev_flag, s);
+	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, op, rb->modulation, in, out,
+	                        fs->num_sms, rb->wide, fs->dev_flag, fs->spin_limit, s);
 }
 
+/* Test hook: removes the batch's tasks of one kind (FGK_TASK_*), so that
+ * the tasks that wait on them run into their bounded waits; the graph is
+ * recorded again at the next execute. */
+int fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind)
+{
+	fgk_task *t;
+	uint32_t i, n = 0;
+	cudaError_t e;
+	if (!rb)
+		return FFTSET_E_INVALID;
+	cudaStreamSynchronize(rb->fs->stream);
+	t = (fgk_task *)malloc(sizeof(*t) * (rb->ntasks ? rb->ntasks : 1));
+	if (!t)
+		return FFTSET_E_NOMEM;
+	if ((e = cudaMemcpy(t, rb->tasks_dev, sizeof(*t) * rb->ntasks, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+		free(t);
+		return fs_cuda(rb->fs, e);
+	}
+	for (i = 0; i < rb->ntasks; i++)
+		if ((int)t[i].kind != kind)
+			t[n++] = t[i];
+	e = cudaMemcpy(rb->tasks_dev, t, sizeof(*t) * n, cudaMemcpyHostToDevice);
+	free(t);
+	if (e != cudaSuccess)
+		return fs_cuda(rb->fs, e);
+	rb->ntasks = n;
+	if (rb->exec) {
+		cudaGraphExecDestroy(rb->exec);
+		rb->exec = NULL;
+	}
+	return FFTSET_OK;
+}
+
+static int fsr_execute(struct fftset_ragged *rb, float *output_base, const float *input_base);
+
+/* Several threads may execute batches of one fftset (and the same batch):
+ * the launch and the graph it may re-instantiate are made under the
+ * fftset's lock; the wait for the results is not. */
 int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)
 {
 	struct fs_impl *fs;
 	int rc;
-	cudaError_t e;
 	if (!rb || !output_base || !input_base)
 		return FFTSET_E_INVALID;
 	fs = rb->fs;
 	if (!fs_is_device_ptr(output_base) || !fs_is_device_ptr(input_base))
 		return fs_latch(fs, FFTSET_E_INVALID, 0); /* ragged batches take device buffers */
+	FS_RANGE_PUSH("fftset_ragged_execute");
+	pthread_mutex_lock(&fs->lock);
+	rc = fsr_execute(rb, output_base, input_base);
+	pthread_mutex_unlock(&fs->lock);
+	if (rc == 0 && fs->blocking && (rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) == 0)
+		rc = fs_check_flag(fs);
+	FS_RANGE_POP();
+	return rc;
+}
+
+static int fsr_execute(struct fftset_ragged *rb, float *output_base, const float *input_base)
+{
+	struct fs_impl *fs = rb->fs;
+	int rc;
+	cudaError_t e;
 	if (!rb->use_graph) {
-		rc = fsr_record(rb, output_base, input_base, fs->stream);
+		rc = fsr_record(rb, rb->op, output_base, input_base, fs->stream);
 		if (rc)
 			return fs_latch(fs, FFTSET_E_CUDA, rc);
 	} else {
@@ -400,11 +463,11 @@ int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const fl
 			/* an uncaptured run on the caller's stream first (ordered with the
 			 * caller's work, same result as the graph): it also sets the
 			 * kernels' shared-memory attributes outside the capture */
-			if ((rc = fsr_record(rb, output_base, input_base, fs->stream)) != 0)
+			if ((rc = fsr_record(rb, rb->op, output_base, input_base, fs->stream)) != 0)
 				return fs_latch(fs, FFTSET_E_CUDA, rc);
 			if ((e = cudaStreamBeginCapture(rb->cap_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
 				return fs_cuda(fs, e);
-			rc = fsr_record(rb, output_base, input_base, rb->cap_stream);
+			rc = fsr_record(rb, rb->op, output_base, input_base, rb->cap_stream);
 			e = cudaStreamEndCapture(rb->cap_stream, &graph);
 			if (rc || e != cudaSuccess) {
 				if (graph)
@@ -422,11 +485,6 @@ int fftset_ragged_execute(struct fftset_ragged *rb, float *output_base, const fl
 		}
 		if ((e = cudaGraphLaunch(rb->exec, fs->stream)) != cudaSuccess)
 			return fs_cuda(fs, e);
-	}
-	if (fs->blocking) {
-		if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) != 0)
-			return rc;
-		return fs_check_flag(fs);
 	}
 	return FFTSET_OK;
 }
@@ -451,23 +509,34 @@ unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb)
 
 /* The plain calls (forward / inverse, device buffers) of a plan beyond the
  * shared-memory limit: `count` items of its size at b * stride, one task
- * launch on `stream`. The task list is kept on the plan for the last (count,
- * strides) seen; the direction is chosen at launch. */
+ * launch on `stream`. The plan keeps the task lists of the last
+ * FS_TASK_LISTS shapes (count, strides) it ran, so that callers alternating
+ * between a few shapes (the adjoint's sub-batches, single calls between
+ * batches) do not rebuild one per call; the direction is a launch argument.
+ * Called with fs->lock held: the lists are shared by all threads calling
+ * this plan, and a list being replaced is freed only after the stream's
+ * earlier launches, which may use it, have finished (fsr_free). */
 int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
                    unsigned count, cudaStream_t stream)
 {
 	struct fs_impl *fs = f->fs;
 	const size_t nf = 2 * (size_t)f->lfft;
+	struct fs_tasklist *t = NULL;
+	unsigned k;
 	if (count == 0)
 		return 0;
 	if (count == 1)
 		in_stride = out_stride = nf;
-	if (!f->tasks || f->tasks_count != count || f->tasks_in_stride != in_stride ||
-	    f->tasks_out_stride != out_stride) {
+	for (k = 0; k < FS_TASK_LISTS && !t; k++)
+		if (f->tl[k].rb && f->tl[k].count == count && f->tl[k].in_stride == in_stride &&
+		    f->tl[k].out_stride == out_stride)
+			t = &f->tl[k];
+	if (!t) {
 		unsigned *bins = (unsigned *)malloc(sizeof(unsigned) * count);
 		size_t *io = (size_t *)malloc(sizeof(size_t) * count), *oo = (size_t *)malloc(sizeof(size_t) * count);
+		struct fftset_ragged *rb;
 		unsigned b;
-		int err0 = fs->err;
+		const int err0 = __atomic_load_n(&fs->err, __ATOMIC_ACQUIRE);
 		if (!bins || !io || !oo) {
 			free(bins);
 			free(io);
@@ -479,26 +548,39 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 			io[b] = b * in_stride;
 			oo[b] = b * out_stride;
 		}
-		fsr_free(f->tasks);
-		f->tasks = fsr_create(fs, f->modulator, op, count, bins, io, oo);
+		rb = fsr_create(fs, f->modulator, op, count, bins, io, oo);
 		free(bins);
 		free(io);
 		free(oo);
-		if (!f->tasks) {
+		if (!rb) {
 			/* no tile split for this size: the caller falls back; leave the
-			 * latched error as it was */
-			if (!err0 && fs->err == FFTSET_E_UNSUPPORTED) {
-				fs->err = 0;
-				fs->cuda_err = 0;
-			}
+			 * latched error as it was. Other failures (memory) are the
+			 * call's. */
+			int unsup = FFTSET_E_UNSUPPORTED;
+			if (fsr_why != FFTSET_E_UNSUPPORTED)
+				return -(fsr_why ? fsr_why : FFTSET_E_NOMEM);
+			if (!err0 && __atomic_compare_exchange_n(&fs->err, &unsup, 0, 0, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE))
+				__atomic_store_n(&fs->cuda_err, 0, __ATOMIC_RELEASE);
 			return -FFTSET_E_UNSUPPORTED;
 		}
-		f->tasks_count = count;
-		f->tasks_in_stride = in_stride;
-		f->tasks_out_stride = out_stride;
+		/* an empty slot, else the least recently used list */
+		t = &f->tl[0];
+		for (k = 0; k < FS_TASK_LISTS; k++) {
+			if (!f->tl[k].rb) {
+				t = &f->tl[k];
+				break;
+			}
+			if (f->tl[k].used < t->used)
+				t = &f->tl[k];
+		}
+		fsr_free(t->rb);
+		t->rb = rb;
+		t->count = count;
+		t->in_stride = in_stride;
+		t->out_stride = out_stride;
 	}
-	f->tasks->op = op; /* the task list does not depend on the direction */
-	return fsr_record(f->tasks, out, in, stream);
+	t->used = ++f->tl_clock;
+	return fsr_record(t->rb, op, out, in, stream);
 }
 
 /* ------------------------------------------------------------------------
@@ -565,11 +647,11 @@ static float fsr_time_size(struct fs_impl *fs, struct fftset_fft *f, int op, uns
 	free(offs);
 	if (!rb)
 		return -1.f;
-	if (fsr_record(rb, buf_out, buf_in, fs->stream) == 0) {
+	if (fsr_record(rb, op, buf_out, buf_in, fs->stream) == 0) {
 		for (r = 0; r < 3; r++) {
 			float ms = 0.f;
 			cudaEventRecord(e0, fs->stream);
-			fsr_record(rb, buf_out, buf_in, fs->stream);
+			fsr_record(rb, op, buf_out, buf_in, fs->stream);
 			cudaEventRecord(e1, fs->stream);
 			if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
 				break;
@@ -622,7 +704,21 @@ int fsr_apply_schedule(struct fs_impl *fs, struct fftset_fft *f, const uint32_t 
 	return FFTSET_OK;
 }
 
+static int fsr_autotune(struct fftset_ragged *rb);
+
+/* Changes the schedules of the fftset's plans: under the fftset's lock. */
 int fftset_ragged_autotune(struct fftset_ragged *rb)
+{
+	int rc;
+	if (!rb || !rb->bins)
+		return FFTSET_E_INVALID;
+	pthread_mutex_lock(&rb->fs->lock);
+	rc = fsr_autotune(rb);
+	pthread_mutex_unlock(&rb->fs->lock);
+	return rc;
+}
+
+static int fsr_autotune(struct fftset_ragged *rb)
 {
 	struct fs_impl *fs;
 	float *bin = NULL, *bout = NULL;
@@ -658,7 +754,7 @@ int fftset_ragged_autotune(struct fftset_ragged *rb)
 			continue;
 		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
 			/* whole items: radix order x threads per item */
-			uint32_t rad[3][FGK_MAX_STAGES], nr[3], nc = 0, c, k, tgs[3], ntg, q;
+			uint32_t rad[3][FGK_MAX_STAGES], nr[3] = {0, 0, 0}, nc = 0, c, k, tgs[3], ntg, q;
 			fgk_plan best_plan = f->rp;
 			void *best_dmem = NULL;
 			uint32_t best_tg = fsr_item_threads(&f->rp);

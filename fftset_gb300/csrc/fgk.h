@@ -178,13 +178,14 @@ int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in,
  * the finished COLS tiles of each big item, the finished A and B tiles of
  * each three-level item) and is reset by the launcher;
  * scratch_dev holds the big items' L1 x L2 intermediates; err_flag is set
- * when a bounded wait gives up; wide selects the CTA shape the list was
- * planned for (0: 128 threads, three CTAs per SM; 1: 256 threads, two) */
+ * when a bounded wait gives up, after spin_limit polls (about 256 ns
+ * apart); wide selects the CTA shape the list was planned for (0: 128
+ * threads, three CTAs per SM; 1: 256 threads, two) */
 int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                         const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                         const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev,
                         float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
-                        int num_sms, int wide, int *err_flag, void *stream);
+                        int num_sms, int wide, int *err_flag, uint32_t spin_limit, void *stream);
 int    fgk_tasks_grid(int num_sms, int wide);
 int    fgk_tasks_threads(int wide);
 /* points of a tile (items up to this size run whole) and the shared-memory

@@ -88,8 +88,10 @@ extern "C" int fftset_fft_execute_fixed_scratch(const struct fftset_fft *fft, in
 	if ((e = fgk_fixed_scratch_address(dev, &scratch)) != cudaSuccess)
 		return fs_cuda(fs, e);
 
+	FS_RANGE_PUSH("fftset_fft_execute_fixed_scratch");
 	rc = fgk_launch_fourstep(&fft->p4, op, output_buf, input_buf, kernel_buf, fft->kidx4, (int)fft->lanes, scratch,
 	                         count, count > 1 ? in_stride : nf, count > 1 ? out_stride : nf, nf, fs->stream);
+	FS_RANGE_POP();
 	if (rc)
 		return fs_latch(fs, FFTSET_E_CUDA, rc);
 	if (fs->blocking) {

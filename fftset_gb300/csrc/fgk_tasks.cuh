@@ -57,7 +57,6 @@ constexpr int TK_THREADS_NARROW = 128, TK_CTAS_NARROW = 3;
 constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 2;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
 constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
-constexpr uint32_t TK_SPIN_LIMIT = 1u << 22;                         /* x 256 ns: about a second */
 
 /* q = w / d for 0 <= w < 2^24, inv = 1/d (one correction step) */
 __device__ __forceinline__ int tk_div(int w, int d, float inv)
@@ -268,9 +267,10 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 }
 
 /* Bounded wait of a whole CTA until *ctr >= need (thread 0 polls with an
- * acquire load, then a barrier). On timeout the error flag is raised and
- * false returned: the caller skips its tile. */
-__device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int *failed)
+ * acquire load, then a barrier), at most spin_limit polls about 256 ns
+ * apart (the host's default, 2^22, is about a second). On timeout the error
+ * flag is raised and false returned: the caller skips its tile. */
+__device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int *failed, uint32_t spin_limit)
 {
 	if (threadIdx.x == 0) {
 		int f = 0;
@@ -280,7 +280,7 @@ __device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int 
 			asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(d) : "l"(ctr) : "memory");
 			if (d >= need)
 				break;
-			if (++it > TK_SPIN_LIMIT) {
+			if (++it > spin_limit) {
 				f = 1;
 				if (err)
 					atomicExch(err, 1);
@@ -417,7 +417,8 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
  * into X[k1 + L1 k2] */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, float *out_base, float2 *scratch,
-                                          const int *done, int *err, float2 *smem, int *failed, Pre &&pre)
+                                          const int *done, int *err, uint32_t spin_limit, float2 *smem, int *failed,
+                                          Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
@@ -428,7 +429,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 	const int tid = (int)threadIdx.x, T = (int)blockDim.x;
 
 	/* every COLS tile of this item, bounded */
-	if (!tk_wait(done, (int)bg.ncols, err, failed))
+	if (!tk_wait(done, (int)bg.ncols, err, failed, spin_limit))
 		return;
 
 	const float2 *Stile = scratch + bg.scratch_off + (uint64_t)tk.a * ((uint64_t)L2 << ls);
@@ -528,7 +529,8 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
  * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
-                                        int *done_b, int *err, float2 *smem, int *failed, Pre &&pre)
+                                        int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
+                                        Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
@@ -539,7 +541,7 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
 	const float2 *A = scratch + hg.sa;
 	float2 *B = scratch + hg.sb;
-	if (!tk_wait(done_a, (int)hg.na, err, failed))
+	if (!tk_wait(done_a, (int)hg.na, err, failed, spin_limit))
 		return;
 	auto ld = [&](int n2, int lane) {
 		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
@@ -565,7 +567,8 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
  * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
-                                        const int *done_b, int *err, float2 *smem, int *failed, Pre &&pre)
+                                        const int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
+                                        Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
@@ -576,7 +579,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 	float *o = out_base + hg.out_off;
 	float2 *o2 = reinterpret_cast<float2 *>(o);
 	const float2 *oa = (const float2 *)p->oa, *ob = (const float2 *)p->ob, *oc = (const float2 *)p->oc;
-	if (!tk_wait(done_b, (int)hg.nb, err, failed))
+	if (!tk_wait(done_b, (int)hg.nb, err, failed, spin_limit))
 		return;
 	auto ld = [&](int n3, int lane) {
 		const int k1 = k1b + lane;
@@ -617,7 +620,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
                 const fgk_huge *__restrict__ huges, int *counters, int *hcounters, float2 *scratch,
-                const float *in_base, float *out_base, int *err)
+                const float *in_base, float *out_base, int *err, uint32_t spin_limit)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
@@ -658,16 +661,16 @@ __global__ void __launch_bounds__(THREADS, MINB)
 		else if (tk.kind == FGK_TASK_COLS)
 			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_ROWS)
-			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, smem,
-			                         &failed, pre);
+			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, spin_limit,
+			                         smem, &failed, pre);
 		else if (tk.kind == FGK_TASK_PA)
 			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_PB)
 			task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref, hcounters + 2 * tk.ref + 1, err,
-			                       smem, &failed, pre);
+			                       spin_limit, smem, &failed, pre);
 		else
-			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, smem,
-			                       &failed, pre);
+			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, spin_limit,
+			                       smem, &failed, pre);
 		if (threadIdx.x == 0) {
 			if (copying) {
 				asm volatile("cp.async.wait_all;" ::: "memory");
@@ -696,7 +699,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
 template <bool inverse, bool freq, int THREADS, int MINB>
 int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans,
                  const fgk_rg_item *items, const fgk_big *bigs, const fgk_huge *huges, int *counters,
-                 int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, cudaStream_t stream)
+                 int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, uint32_t spin_limit,
+                 cudaStream_t stream)
 {
 	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
 	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq, THREADS, MINB>,
@@ -704,7 +708,8 @@ int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fg
 	if (e != cudaSuccess)
 		return (int)e;
 	task_kernel<inverse, freq, THREADS, MINB><<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
-	                                                              hcounters, scratch, in_base, out_base, err);
+	                                                              hcounters, scratch, in_base, out_base, err,
+	                                                              spin_limit);
 	return (int)cudaGetLastError();
 }
 
@@ -713,5 +718,7 @@ int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fg
 #define FGKT_LAUNCH_ARGS                                                                                 \
 	uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans, const fgk_rg_item *items,     \
 	    const fgk_big *bigs, const fgk_huge *huges, int *counters, int *hcounters, float2 *scratch,              \
-	    const float *in_base, float *out_base, int *err, cudaStream_t stream
-#define FGKT_LAUNCH_PASS grid, tasks, ntasks, plans, items, bigs, huges, counters, hcounters, scratch, in_base, out_base, err, stream
+	    const float *in_base, float *out_base, int *err, uint32_t spin_limit, cudaStream_t stream
+#define FGKT_LAUNCH_PASS                                                                                 \
+	grid, tasks, ntasks, plans, items, bigs, huges, counters, hcounters, scratch, in_base, out_base, err, spin_limit, \
+	    stream

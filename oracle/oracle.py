@@ -388,7 +388,8 @@ class PortPlan:
 
 # --------------------------------------------------------------------------
 # The unmodified reference compiled here (only where its sources exist).
-REF_SOURCES = "/root/reference"
+# FFTSET_REFERENCE_SRC, the default being where this container mounts them
+REF_SOURCES = os.environ.get("FFTSET_REFERENCE_SRC", "/root/reference")
 
 
 def build_reference() -> bool:

@@ -440,10 +440,12 @@ def test_fourstep_large_single(gpu_set):
     Xh = host(X).astype(np.float64)
     want = O.freqoff_forward64(x)
     assert O.rel_l2(Xh, want) <= tol(1, L)
+    # every band of L/8 bins within the tolerance itself (measured 1.9-2.6e-7
+    # per band, against 5e-5)
     bands = np.array_split(np.arange(L), 8)
     for b in bands:
         sl = np.concatenate([2 * b, 2 * b + 1])
-        assert O.rel_l2(Xh[sl], want[sl]) <= 10 * tol(1, L)
+        assert O.rel_l2(Xh[sl], want[sl]) <= tol(1, L)
     r = torch.empty(2 * L, device="cuda")
     f.inverse(r, X)
     assert O.rel_l2(host(r) / L, x) <= tol(1, L)

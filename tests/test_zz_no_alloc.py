@@ -6,8 +6,11 @@ driver's allocator. It runs the four-step passes of sizes beyond the
 shared-memory limit with their work buffer in a fixed device array. Its
 results must equal the regular batched call's (fftset_fft_*_batch) on two
 calls in a row, the second one reusing what the first left in the array, and
-it must refuse what it cannot run within the array. Tolerance: relative L2
-<= 2e-6 * log2(N), as in the other parity tests.
+it must refuse what it cannot run within the array. Each result is also
+checked against the FP64 oracle directly (the regular batched forward and
+inverse run other kernels, so the comparison between the two GPU paths
+alone would pin this one only indirectly). Tolerance: relative L2 <=
+2e-6 * log2(N), as in the other parity tests.
 
 This file is named to be collected last, and it makes its own fftset, so it
 passes alone in a fresh process as well as after the other tests."""
@@ -21,7 +24,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 FFTSET_OK, FFTSET_E_INVALID, FFTSET_E_UNSUPPORTED = 0, 1, 4
-OPS = {"forward": 0, "inverse": 1, "conv": 3}
+OPS = {"forward": 0, "inverse": 1, "get_kernel": 2, "conv": 3, "corr": 4}
 
 
 def _entry(lib):
@@ -52,27 +55,41 @@ def test_fixed_scratch_matches_batched_call(fftset_lib, fset, mod, L, count):
     assert f is not None
     fset.set_stream(torch.cuda.current_stream())
     rng = np.random.default_rng(100 + L + mod)
-    h = torch.from_numpy(rng.standard_normal(2 * L).astype(np.float32)).cuda()
+    h_np = rng.standard_normal(2 * L).astype(np.float32)
+    h = torch.from_numpy(h_np).cuda()
     K = torch.empty(2 * L, device="cuda")
     f.conv_get_kernel(K, h)
     for call in range(2):
-        x = torch.from_numpy(rng.standard_normal((count, 2 * L)).astype(np.float32)).cuda()
+        x_np = rng.standard_normal((count, 2 * L)).astype(np.float32)
+        x = torch.from_numpy(x_np).cuda()
         for name, op in OPS.items():
             want = torch.empty_like(x)
             if name == "forward":
                 f.forward_batch(want, x)
+                want64 = O.forward64(mod, x_np)
             elif name == "inverse":
                 f.inverse_batch(want, x)
-            else:
+                want64 = O.inverse64(mod, x_np)
+            elif name == "get_kernel":
+                f.conv_get_kernel_batch(want, x)
+                want64 = np.stack([O.kernel_from_spectrum(mod, O.spectrum64(mod, r), 4) for r in x_np])
+            elif name == "conv":
                 f.conv_batch(want, x, K)
+                want64 = O.conv64(mod, x_np, h_np[None, :])
+            else:
+                gi = torch.empty_like(x)
+                f.conv_adjoint_batch(gi, None, x, x, K)
+                want = gi
+                want64 = O.conv64(mod, x_np, O.reverse(mod, h_np.astype(np.float64))[None, :])
             got = torch.full_like(x, float("nan"))
             rc = fn(f.handle, op, got.data_ptr(), 2 * L, x.data_ptr(), 2 * L,
-                    K.data_ptr() if name == "conv" else None, count)
+                    K.data_ptr() if name in ("conv", "corr") else None, count)
             torch.cuda.synchronize()
             assert rc == FFTSET_OK, (call, name, fftset_lib.error_string(rc))
             g, w = got.cpu().numpy(), want.cpu().numpy()
             assert np.all(np.isfinite(g)), (call, name)
             assert O.rel_l2(g, w) <= _tol(mod, L), (call, name)
+            assert O.rel_l2(g, want64) <= _tol(mod, L), (call, name, O.rel_l2(g, want64))
     assert fset.last_error() == 0
 
 
