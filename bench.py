@@ -525,13 +525,18 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    import ctypes
+    launch_count = fs.library().fftset__launch_count
+    launch_count.restype = ctypes.c_ulonglong
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    n0 = launch_count()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
+    launches = int(launch_count() - n0)  # the library's own kernel launches in the timed region
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
@@ -581,7 +586,7 @@ def run_gb300(args):
             "e2e": {"value": job_gbs(world, e2e_s), "unit": "GB/s",
                     "h2d_bytes_per_step": int(x_np.nbytes), "d2h_bytes_per_step": int(x_np.nbytes),
                     "parity_ok": bool(e2e_ok)},
-            "gpu_launches": args.steps,
+            "gpu_launches": launches,
             "clocks": clocks,
             "workloads": others,
         }
@@ -616,6 +621,8 @@ def profile_case(args):
         torch.cuda.synchronize()
         S.check()
         print(json.dumps({"profile": "ragged", "items": len(sizes), "bytes": rb.bytes}))
+    elif args.profile == "kernels":
+        profile_kernels(torch, fs)
     elif args.profile == "large":
         L = 15728640
         S = fs.FftSet()
@@ -632,6 +639,116 @@ def profile_case(args):
         print(json.dumps({"profile": "large", "bins": L}))
 
 
+def profile_kernels(torch, fs):
+    """Every kernel of the library on one case each, each case run twice (the
+    second run is the one an ncu launch list reads), device buffers: prints
+    one JSON object per case, in launch order, with its algorithmic bytes
+    (one read of every input block, one write of every output block; the
+    kernel spectrum once) and the library kernels it launches per run."""
+    S = fs.FftSet()
+    st = torch.cuda.current_stream()
+    S.set_stream(st)
+    S.set_blocking(False)
+    rng = np.random.default_rng(11)
+    cases = []
+
+    import ctypes
+    count = fs.library().fftset__launch_count
+    count.restype = ctypes.c_ulonglong
+
+    def run(name, fn, nbytes, launches):
+        c0 = count()
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        c1 = count()
+        S.check()
+        assert c1 - c0 == 2 * launches, (name, c1 - c0)
+        # library launch indices of the second run (the n-th library launch of
+        # the process is the n-th kernel an ncu capture filtered to the
+        # library's kernels lists)
+        cases.append({"case": name, "bytes": int(nbytes), "launches": [c0 + launches, c1]})
+
+    def buf(n):
+        return torch.from_numpy(rng.standard_normal(n).astype(np.float32)).cuda()
+
+    # generic resident kernel (a size without compiled kernels): 1 block and
+    # 16384 blocks (268 MB per buffer, above L2)
+    f = S.create_fft(fs.COMPLEX, 2048)
+    x1, y1 = buf(4096), torch.empty(4096, device="cuda")
+    run("resident_generic COMPLEX 2048 forward x1", lambda: f.forward(y1, x1), 2 * 16384, 1)
+    x, y = buf(16384 * 4096).view(16384, 4096), torch.empty(16384, 4096, device="cuda")
+    run("resident_generic COMPLEX 2048 forward x16384", lambda: f.forward_batch(y, x), 2 * x.numel() * 4, 1)
+    del x, y
+    # compiled kernels, forward / inverse / conv, above L2
+    for mod, L, B in ((fs.FREQ_OFFSET_REAL, 1536, 16384), (fs.FREQ_OFFSET_REAL, 4096, 8192),
+                      (fs.COMPLEX, 1024, 32768), (fs.COMPLEX, 4096, 8192)):
+        g = S.create_fft(mod, L)  # default variants: the fastest measured first
+        name = ("FREQ" if mod == fs.FREQ_OFFSET_REAL else "COMPLEX") + f" {L} x{B}"
+        x, y = buf(B * 2 * L).view(B, 2 * L), torch.empty(B, 2 * L, device="cuda")
+        K = torch.empty(2 * L, device="cuda")
+        g.conv_get_kernel(K, buf(2 * L))
+        run(f"static forward {name} (variant {g.variant(fs.OP_FORWARD)})", lambda: g.forward_batch(y, x),
+            2 * x.numel() * 4, 1)
+        run(f"static inverse {name} (variant {g.variant(fs.OP_INVERSE)})", lambda: g.inverse_batch(y, x),
+            2 * x.numel() * 4, 1)
+        run(f"static conv {name} (variant {g.variant(fs.OP_CONV)})", lambda: g.conv_batch(y, x, K),
+            2 * x.numel() * 4 + 8 * L, 1)
+        del x, y
+    # adjoint: dL/dx (correlation through the conv kernels) and dL/dtaps
+    # (the taps-gradient kernel, kg_reduce, one inverse)
+    g = S.create_fft(fs.FREQ_OFFSET_REAL, 4096)
+    B, nf = 2048, 8192
+    x, w = buf(B * nf).view(B, nf), buf(B * nf).view(B, nf)
+    K, dh, dx = torch.empty(nf, device="cuda"), torch.empty(nf, device="cuda"), torch.empty(B, nf, device="cuda")
+    g.conv_get_kernel(K, buf(nf))
+    run("adjoint dL/dx FREQ 4096 x2048", lambda: g.conv_adjoint_batch(dx, None, w, x, K), 2 * B * nf * 4 + 4 * nf, 1)
+    run("adjoint dL/dtaps FREQ 4096 x2048", lambda: g.conv_adjoint_batch(None, dh, w, x, K), 2 * B * nf * 4 + 4 * nf,
+        3)
+    del x, w, dx
+    # two-pass kernels: convolution beyond the shared-memory limit
+    h = S.create_fft(fs.FREQ_OFFSET_REAL, 65536)
+    B, nf = 512, 131072
+    x, y = buf(B * nf).view(B, nf), torch.empty(B, nf, device="cuda")
+    K = torch.empty(nf, device="cuda")
+    h.conv_get_kernel(K, buf(nf))
+    run("fourstep conv FREQ 65536 x512 (pass 1, 2 of the forward; pass 1, 2 of the inverse)",
+        lambda: h.conv_batch(y, x, K), 2 * B * nf * 4 + 4 * nf, 4)
+    run("task_kernel forward FREQ 65536 x512 (two-level)", lambda: h.forward_batch(y, x), 2 * B * nf * 4, 1)
+    run("task_kernel inverse FREQ 65536 x512 (two-level)", lambda: h.inverse_batch(y, x), 2 * B * nf * 4, 1)
+    del x, y
+    # overlap-add: split, conv, merge over 32 M samples with 1025 taps
+    o = S.create_fft(fs.FREQ_OFFSET_REAL, 1536)
+    n, taps = 32 << 20, 1025
+    sig, res = buf(n), torch.empty(n + taps - 1, device="cuda")
+    K = torch.empty(3072, device="cuda")
+    o.conv_get_kernel(K, torch.cat([buf(taps), torch.zeros(3072 - taps, device="cuda")]))
+    run("overlap-add FREQ 1536, 32 M samples, 1025 taps", lambda: o.conv_overlap_add(res, sig, K, taps),
+        8 * n, 3)
+    del sig, res
+    # ragged batch (first 2000 items of the ragged draw) and the
+    # 15,728,640-bin transform (three-level)
+    sizes = [int(v) for v in ragged_sizes(20000, 4)[:2000]]
+    offs, tot = [], 0
+    for v in sizes:
+        offs.append(tot)
+        tot += 2 * v
+    x, y = buf(tot), torch.empty(tot, device="cuda")
+    rb = fs.Ragged(S, fs.COMPLEX, fs.OP_FORWARD, sizes, offs, offs)
+    rb.set_graph(False)
+    run("task_kernel ragged COMPLEX forward, 2000 items 60..65536", lambda: rb.execute(y, x), rb.bytes, 1)
+    rb.close()
+    del x, y
+    Lg = 15728640
+    big = S.create_fft(fs.FREQ_OFFSET_REAL, Lg)
+    x, X = buf(2 * Lg), torch.empty(2 * Lg, device="cuda")
+    run("task_kernel forward FREQ 15728640 (three-level)", lambda: big.forward(X, x), 16 * Lg, 1)
+    run("task_kernel inverse FREQ 15728640 (three-level)", lambda: big.inverse(x, X), 16 * Lg, 1)
+    S.close()
+    for c in cases:
+        print(json.dumps(c))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -642,8 +759,9 @@ def main():
                     help="only the headline workload (no per-call, ragged, large and adjoint lines)")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin the conv kernel variant (-1 generic) instead of autotuning")
-    ap.add_argument("--profile", choices=["ragged", "large"], default=None,
-                    help="run one small fixed case for an ncu capture instead of the benchmark")
+    ap.add_argument("--profile", choices=["ragged", "large", "kernels"], default=None,
+                    help="run one small fixed case for an ncu capture instead of the benchmark "
+                         "(kernels: every library kernel on one case each)")
     ap.add_argument("--items", type=int, default=2000, help="items of the --profile ragged case")
     args = ap.parse_args()
     if args.profile:

@@ -9,8 +9,12 @@
  *                  the negacyclic (FREQ_OFFSET_REAL) or cyclic (COMPLEX)
  *                  cross-correlation of g_b with h;
  *   grad_taps    = inverse( sum_b G_b conj(X_b) ), the gradient with respect
- *                  to the taps h: batched forward transforms of g and x into
- *                  scratch, column sums (fgk_adjoint.cu), the plan's inverse.
+ *                  to the taps h: where the size has a compiled taps-gradient
+ *                  kernel (fgk_static.cuh, static_kernel_kgrad), one pass that
+ *                  transforms both blocks of every pair and accumulates the
+ *                  product per CTA; otherwise batched forward transforms of
+ *                  g and x into scratch and column sums (fgk_adjoint.cu);
+ *                  then the row sums and the plan's inverse.
  * For FREQ_OFFSET_REAL (real data) these are the gradients of a real loss;
  * for COMPLEX they are the adjoint linear maps. */
 #include <stdint.h>
@@ -41,6 +45,36 @@ static int fsa_rc(struct fs_impl *fs, int rc)
 	if (rc == 0)
 		return FFTSET_OK;
 	return rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
+}
+
+/* grad_taps through the compiled taps-gradient kernel (sizes that have
+ * one): every block pair transformed and multiplied in shared memory and
+ * registers, one partial row per CTA, the rows summed into the
+ * FREQ_OFFSET_REAL forward layout (or natural order), then the inverse.
+ * Returns -FFTSET_E_UNSUPPORTED when the size has no such kernel. */
+static int fsa_taps_fused(const struct fftset_fft *f, float *grad_taps, const float *g, size_t g_stride,
+                          const float *x, size_t x_stride, unsigned count)
+{
+	struct fs_impl *fs = f->fs;
+	const size_t L = f->lfft, nf = 2 * L;
+	const int v = fgk_static_kgrad_variant(f->rp.modulation, (uint32_t)L);
+	const uint32_t cap = 4u * (uint32_t)fs->num_sms;
+	uint32_t rows = 0;
+	float *partials, *S;
+	int rc;
+	if (v < 0 || v >= f->nvar)
+		return -FFTSET_E_UNSUPPORTED;
+	if ((rc = fs_stage_reserve(fs, FSA_SLOT, ((size_t)cap + 1) * nf * sizeof(float))) != 0)
+		return -rc;
+	partials = (float *)fs->stage[FSA_SLOT];
+	S = partials + (size_t)cap * nf;
+	if ((rc = fgk_launch_static_kgrad(&f->vp[v], v, g, g_stride, x, x_stride, count, partials, cap, &rows, fs->stream,
+	                                  fs->num_sms)) != 0)
+		return rc < 0 ? -FFTSET_E_UNSUPPORTED : rc;
+	if ((rc = fgk_launch_kgrad_reduce(partials, rows, (uint32_t)L, f->modulator->freq_offset_real, S, fs->stream)) !=
+	    0)
+		return rc;
+	return fs_launch(f, FGK_OP_INVERSE, grad_taps, S, NULL, 1, 0, 0);
 }
 
 /* grad_taps: batched forward transforms into scratch, column sums of
@@ -135,7 +169,9 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 			goto done;
 	}
 	if (grad_taps) {
-		rc = fsa_taps(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
+		rc = fsa_taps_fused(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
+		if (rc == -FFTSET_E_UNSUPPORTED)
+			rc = fsa_taps(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
 		if ((rc = fsa_rc(fs, rc)) != 0)
 			goto done;
 	}

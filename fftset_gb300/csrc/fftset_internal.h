@@ -47,10 +47,12 @@ struct fftset_fft {
 	void                           *dmem3; /* its device tables */
 	/* task lists of the plain calls of this plan (fftset_ragged.c), one per
 	 * (count, strides) shape seen, least recently used replaced first; the
-	 * direction is a launch argument, so a list serves both. Read and
+	 * direction is a launch argument, so a COMPLEX list serves both (op -1;
+	 * FREQ_OFFSET_REAL lists are ordered for one direction, op). Read and
 	 * written with fs->lock held. */
 	struct fs_tasklist {
 		struct fftset_ragged *rb;
+		int                   op;
 		unsigned              count;
 		size_t                in_stride, out_stride;
 		uint64_t              used;

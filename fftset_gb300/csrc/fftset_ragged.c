@@ -258,16 +258,27 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	tasks = (fgk_task *)malloc(sizeof(*tasks) * (cap_tasks ? cap_tasks : 1));
 	if (!tasks)
 		goto fail;
+	/* FREQ_OFFSET_REAL keeps bin m and its mirror L-1-m in one 16-byte pair
+	 * (X[2m] = W[m], X[2m+1] = conj W[L-1-m]): the tiles writing the
+	 * forward's output (ROWS, C) and those reading the inverse's input
+	 * (COLS, A) are listed next to their mirror tile, the one holding the
+	 * mirrored bins (tile t of N mirrors tile N-1-t), so that both halves
+	 * of every pair meet in L2 within microseconds and reach HBM as whole
+	 * sectors instead of two partial writes (or reads) far apart. */
+	const int zip_in = rb->modulation == FGK_MOD_FREQOFF && op == FFTSET_OP_INVERSE;
+	const int zip_out = rb->modulation == FGK_MOD_FREQOFF && op == FFTSET_OP_FORWARD;
+#define FSR_ZIP(on, k, N) ((on) ? (((k) & 1) ? (N) - 1 - ((k) >> 1) : ((k) >> 1)) : (k))
 	/* three-level items: all A tiles, all B tiles, all C tiles */
 	for (i = 0; i < nhuge; i++) {
 		const struct fftset_fft *f = fs_create_plan(fs, modulation, order[i].bins);
+		const uint32_t nc = huges[i].nc1 * f->p3.L2;
 		uint32_t t;
 		for (t = 0; t < huges[i].na; t++)
-			tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, t, 0};
+			tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, FSR_ZIP(zip_in, t, huges[i].na), 0};
 		for (t = 0; t < huges[i].nb; t++)
 			tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, t, 0};
-		for (t = 0; t < huges[i].nc1 * f->p3.L2; t++)
-			tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i, t, 0};
+		for (t = 0; t < nc; t++)
+			tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i, FSR_ZIP(zip_out, t, nc), 0};
 	}
 	/* big items: COLS of item b, ROWS of item b - D */
 	if (nbig) {
@@ -277,12 +288,13 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		for (b = 0; b < nbig + D; b++) {
 			if (b < nbig)
 				for (t = 0; t < bigs[b].ncols; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_COLS, b, t, 0};
+					tasks[ntasks++] = (fgk_task){FGK_TASK_COLS, b, FSR_ZIP(zip_in, t, bigs[b].ncols), 0};
 			if (b >= D)
 				for (t = 0; t < bigs[b - D].nrows; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_ROWS, b - D, t, 0};
+					tasks[ntasks++] = (fgk_task){FGK_TASK_ROWS, b - D, FSR_ZIP(zip_out, t, bigs[b - D].nrows), 0};
 		}
 	}
+#undef FSR_ZIP
 	/* small items, largest first */
 	{
 		uint32_t pi = 0;
@@ -527,9 +539,12 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 		return 0;
 	if (count == 1)
 		in_stride = out_stride = nf;
+	/* FREQ_OFFSET_REAL lists order their tiles for one direction (mirror
+	 * pairs, fsr_create); COMPLEX lists serve both */
+	const int key_op = f->modulator->freq_offset_real ? op : -1;
 	for (k = 0; k < FS_TASK_LISTS && !t; k++)
 		if (f->tl[k].rb && f->tl[k].count == count && f->tl[k].in_stride == in_stride &&
-		    f->tl[k].out_stride == out_stride)
+		    f->tl[k].out_stride == out_stride && f->tl[k].op == key_op)
 			t = &f->tl[k];
 	if (!t) {
 		unsigned *bins = (unsigned *)malloc(sizeof(unsigned) * count);
@@ -578,6 +593,7 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 		t->count = count;
 		t->in_stride = in_stride;
 		t->out_stride = out_stride;
+		t->op = key_op;
 	}
 	t->used = ++f->tl_clock;
 	return fsr_record(t->rb, op, out, in, stream);

@@ -148,6 +148,12 @@ typedef struct fgk_big {
 	uint32_t                nrows;           /* ROWS tiles */
 } fgk_big;
 
+/* Every kernel launch of the library is counted (fgk_resident.cu): the
+ * counter lets a profile run map the library's launches to its cases and a
+ * benchmark report how many of its own kernels ran. */
+void fgk_count_launch(void);
+unsigned long long fftset__launch_count(void);
+
 /* Host-side planning helpers implemented in fgk_plan.c */
 int  fgk_plan_chain(uint32_t L, uint32_t *radices, uint32_t *nstages);
 /* forced_radices: NULL, or the chain a static kernel was compiled for */
@@ -206,6 +212,17 @@ int fgk_static_info(uint32_t modulation, uint32_t L, int v, uint32_t *radices, u
  * kernel gives up (may be NULL) */
 int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
                       uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms, int *err_flag);
+
+/* The taps-gradient kernel of the adjoint (fgk_static.cuh,
+ * static_kernel_kgrad): the first compiled variant of (modulation, L) that
+ * has one, or -1; the launch writes *rows <= max_rows partial rows of L
+ * float2, P[m] = sum over its blocks of W_g[m] conj(W_x[m]) (natural-order
+ * spectra before the FREQ_OFFSET_REAL split). The plan must be the
+ * variant's (its chain's twiddles). Returns -1 when the variant has none. */
+int fgk_static_kgrad_variant(uint32_t modulation, uint32_t L);
+int fgk_launch_static_kgrad(const fgk_plan *p, int v, const float *g, size_t g_stride, const float *x,
+                            size_t x_stride, uint32_t count, float *partials, uint32_t max_rows, uint32_t *rows,
+                            void *stream, int num_sms);
 
 #ifdef __cplusplus
 }

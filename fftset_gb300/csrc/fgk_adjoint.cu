@@ -69,6 +69,7 @@ extern "C" int fgk_launch_kgrad_spec(const float *S, const float *X, size_t stri
 	kg_spec_partial<<<grid, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2 *>(S),
 	                                                        reinterpret_cast<const float2 *>(X), stride / 2, count, L,
 	                                                        chunk, reinterpret_cast<float2 *>(partials));
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }
 
@@ -78,5 +79,6 @@ extern "C" int fgk_launch_kgrad_reduce(const float *partials, uint32_t P, uint32
 	using namespace fgk;
 	kg_reduce<<<(L + 63) / 64, 64, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2 *>(partials), P, L, pack,
 	                                                          reinterpret_cast<float2 *>(out));
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }

@@ -331,10 +331,12 @@ static int launch_pass(const fgk_plan4 *p, int in_mode, int out_mode, float *out
 		return (int)cudaErrorInvalidValue;
 	k1<<<(unsigned)b1, p->threads1, sm1, stream>>>(*p, in_mode, in, reinterpret_cast<float2 *>(work), count, in_stride,
 	                                                 work_stride / 2);
+	fgk_count_launch();
 	if ((e = cudaGetLastError()) != cudaSuccess)
 		return (int)e;
 	k2<<<(unsigned)b2, p->threads2, sm2, stream>>>(*p, out_mode, reinterpret_cast<const float2 *>(work), out, count,
 	                                                 work_stride / 2, out_stride, kern, kidx, kvw);
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }
 

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fgk.h"
+
 namespace fgk {
 
 /* blocks[b][i] = in[b B + i] for i < B and b B + i < n, else 0 */
@@ -80,6 +82,7 @@ extern "C" int fgk_launch_ola_split(const float *in, uint64_t n, uint32_t B, uin
 		                                                         nblocks, reinterpret_cast<float2 *>(blocks));
 	else
 		ola_split<float><<<grid, 256, 0, (cudaStream_t)stream>>>(in, n, B, N, nblocks, blocks);
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }
 
@@ -93,5 +96,6 @@ extern "C" int fgk_launch_ola_merge(const float *ys, uint32_t B, uint32_t N, uin
 		                                                         nblocks, nout, reinterpret_cast<float2 *>(out));
 	else
 		ola_merge<float><<<grid, 256, 0, (cudaStream_t)stream>>>(ys, B, N, span, nblocks, nout, out);
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }

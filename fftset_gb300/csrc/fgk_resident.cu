@@ -271,6 +271,18 @@ typedef void (*resident_fn)(const fgk_plan, int, float *, const float *, const f
 
 } /* namespace fgk */
 
+static unsigned long long fgk_launches;
+
+extern "C" void fgk_count_launch(void)
+{
+	__atomic_fetch_add(&fgk_launches, 1ull, __ATOMIC_RELAXED);
+}
+
+extern "C" unsigned long long fftset__launch_count(void)
+{
+	return __atomic_load_n(&fgk_launches, __ATOMIC_RELAXED);
+}
+
 extern "C" uint32_t fgk_max_resident_L(void)
 {
 	return 26244u; /* largest 2^a 3^b 5^c whose padded buffer fits 227 KB */
@@ -296,5 +308,6 @@ extern "C" int fgk_launch_resident(const fgk_plan *p, int op, float *out, const 
 	if (blocks > 0x7fffffffull)
 		return (int)cudaErrorInvalidValue;
 	fn<<<(unsigned)blocks, threads, smem, (cudaStream_t)stream>>>(*p, op, out, in, kern, count, in_stride, out_stride);
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }

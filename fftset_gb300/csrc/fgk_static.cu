@@ -1,5 +1,7 @@
 /* Registry and launcher of the compile-time kernels (fgk_static.cuh); the
  * configurations themselves are instantiated in fgk_static_<size>.cu. */
+#include <pthread.h>
+
 #include "fgk_static.cuh"
 
 namespace fgk {
@@ -55,6 +57,45 @@ extern "C" int fgk_static_info(uint32_t mod, uint32_t L, int v, uint32_t *radice
 	return 1;
 }
 
+/* The shared-memory attribute and the occupancy of a kernel, set and
+ * queried once per (kernel, device) and remembered: a launch of a single
+ * small transform then costs no more host calls than the launch itself. */
+namespace fgk {
+struct SetupEntry {
+	const void *fn;
+	int         dev, per_sm;
+	size_t      smem;
+};
+static SetupEntry setup_cache[128];
+static pthread_mutex_t setup_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static cudaError_t launch_setup(const void *fn, int threads, size_t smem, int *per_sm)
+{
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess)
+		return e;
+	pthread_mutex_lock(&setup_lock);
+	for (auto &c : setup_cache)
+		if (c.fn == fn && c.dev == dev && c.smem == smem) {
+			*per_sm = c.per_sm;
+			pthread_mutex_unlock(&setup_lock);
+			return cudaSuccess;
+		}
+	e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e == cudaSuccess)
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, threads, smem);
+	if (e == cudaSuccess)
+		for (auto &c : setup_cache)
+			if (c.fn == nullptr) {
+				c = SetupEntry{fn, dev, *per_sm, smem};
+				break;
+			}
+	pthread_mutex_unlock(&setup_lock);
+	return e;
+}
+} /* namespace fgk */
+
 extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
                                  uint32_t count, size_t in_stride, size_t out_stride, void *stream, int num_sms,
                                  int *err_flag)
@@ -71,11 +112,8 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 	if (count == 0)
 		return 0;
 	const size_t smem = e->smem[op];
-	cudaError_t err = cudaFuncSetAttribute((const void *)e->fn[op], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-	if (err != cudaSuccess)
-		return (int)err;
 	int per_sm = 0;
-	err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)e->fn[op], (int)(e->T * e->G), smem);
+	cudaError_t err = launch_setup((const void *)e->fn[op], (int)(e->T * e->G), smem, &per_sm);
 	if (err != cudaSuccess)
 		return (int)err;
 	if (per_sm < 1)
@@ -86,5 +124,47 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 		grid = need;
 	StaticArgs a{out, in, kern, count, in_stride, out_stride, err_flag};
 	e->fn[op]<<<(unsigned)grid, e->T * e->G, smem, (cudaStream_t)stream>>>(*p, a);
+	fgk_count_launch();
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fgk_static_kgrad_variant(uint32_t mod, uint32_t L)
+{
+	const fgk::StaticEntry *e;
+	const int nv = fgk::variants(mod, L, &e);
+	for (int v = 0; v < nv; v++)
+		if (e[v].kgrad)
+			return v;
+	return -1;
+}
+
+extern "C" int fgk_launch_static_kgrad(const fgk_plan *p, int v, const float *g, size_t g_stride, const float *x,
+                                       size_t x_stride, uint32_t count, float *partials, uint32_t max_rows,
+                                       uint32_t *rows, void *stream, int num_sms)
+{
+	using namespace fgk;
+	const StaticEntry *e;
+	const int nv = variants(p->modulation, p->L, &e);
+	if (v < 0 || v >= nv || !e[v].kgrad)
+		return -1;
+	e += v;
+	int per_sm = 0;
+	cudaError_t err = launch_setup((const void *)e->kgrad, (int)(e->T * e->G), e->kgrad_smem, &per_sm);
+	if (err != cudaSuccess)
+		return (int)err;
+	if (per_sm < 1)
+		return (int)cudaErrorInvalidConfiguration;
+	uint64_t grid = (uint64_t)per_sm * (uint64_t)num_sms;
+	const uint64_t need = ((uint64_t)count + e->G - 1) / e->G;
+	if (grid > need)
+		grid = need;
+	if (grid > max_rows)
+		grid = max_rows;
+	if (grid == 0)
+		return (int)cudaErrorInvalidValue;
+	KgradArgs a{g, x, g_stride, x_stride, count, reinterpret_cast<float2 *>(partials)};
+	e->kgrad<<<(unsigned)grid, e->T * e->G, e->kgrad_smem, (cudaStream_t)stream>>>(*p, a);
+	fgk_count_launch();
+	*rows = (uint32_t)grid;
 	return (int)cudaGetLastError();
 }

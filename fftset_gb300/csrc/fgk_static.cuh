@@ -783,15 +783,126 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_pp(const fgk_plan
 	}
 }
 
+/* ---- gradient with respect to the taps --------------------------------- */
+/* For pairs (g_b, x_b) of blocks: P[m] = sum_b W_g,b[m] conj(W_x,b[m]), the
+ * forward transforms' natural-order spectra before the FREQ_OFFSET_REAL
+ * split, accumulated per CTA. Each group transforms g_b, parks the last
+ * stage's outputs in its own buffer (the thread that writes a bin is the
+ * one that reads it back, so no barrier guards it), transforms x_b and
+ * accumulates the products in registers; at the end the groups' sums are
+ * added and the CTA writes one row of `partials`. Every block pair crosses
+ * HBM once (one read of g_b and of x_b); the partial rows are what is left
+ * to reduce (fgk_adjoint.cu, kg_reduce). */
+struct KgradArgs {
+	const float *g, *x;
+	size_t       g_stride, x_stride;
+	uint32_t     count;
+	float2      *partials; /* gridDim.x rows of L */
+};
+
+/* the forward chain of one block up to the last stage's butterflies, whose
+ * outputs (bin j + q L/R of butterfly j) stay in t; ends with `ex` free */
+template <class C, class First>
+__device__ __forceinline__ void forward_to_tile(int tid, int g, const Ex<C> &ex, const First &first,
+                                                const float2 *tws, Tile<C, C::fr(C::N - 1)> &t)
+{
+	constexpr int N = C::N;
+	static_assert(N >= 2, "the gradient kernel needs two or more stages");
+	{
+		constexpr int R = C::fr(0);
+		Tile<C, R> t0;
+		t0.load(tid, first);
+		t0.template butterfly<1>(tid, tws);
+		t0.template store<1>(tid, [&](int i, float2 v) { ex.put(i, v); });
+		gsync<C>(g);
+	}
+	fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
+	t.load(tid, ex);
+	gsync<C>(g);
+	t.template butterfly<C::fns(N - 1)>(tid, tws + C::ftw_off(N - 1));
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_kgrad(const fgk_plan p, KgradArgs a)
+{
+	extern __shared__ float2 smem[];
+	using Lay = Layout<C, FGK_OP_FORWARD>;
+	constexpr int L = C::L, R = C::fr(C::N - 1), NBF = L / R;
+	using TL = Tile<C, R>;
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *exb = mods + Lay::MODS;
+	float2 *park = exb + (size_t)C::G * C::SLOTS; /* G x L */
+	stage_tables<C, FGK_OP_FORWARD>(p, StaticArgs{}, smem, mods, nullptr);
+	__syncthreads();
+
+	const int g = threadIdx.x / C::T;
+	const int tid = C::wt((int)threadIdx.x - g * C::T, g);
+	const Ex<C> ex{exb + (size_t)g * C::SLOTS};
+	float2 *pk = park + (size_t)g * L;
+	float2 acc[TL::NB][R];
+#pragma unroll
+	for (int b = 0; b < TL::NB; b++)
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			acc[b][q] = make_float2(0.f, 0.f);
+	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {
+		{
+			TL tg;
+			forward_to_tile<C>(tid, g, ex, FirstLoad<C, FGK_OP_FORWARD, false>{a.g + t * a.g_stride, mods}, tws, tg);
+#pragma unroll
+			for (int b = 0; b < TL::NB; b++)
+				if (TL::live(tid, b))
+#pragma unroll
+					for (int q = 0; q < R; q++)
+						pk[tid + b * C::T + q * NBF] = tg.v[b][q];
+		}
+		TL tx;
+		forward_to_tile<C>(tid, g, ex, FirstLoad<C, FGK_OP_FORWARD, false>{a.x + t * a.x_stride, mods}, tws, tx);
+#pragma unroll
+		for (int b = 0; b < TL::NB; b++)
+			if (TL::live(tid, b))
+#pragma unroll
+				for (int q = 0; q < R; q++) {
+					const int i = tid + b * C::T + q * NBF;
+					acc[b][q] = cadd(acc[b][q], cmulc(pk[i], tx.v[b][q]));
+				}
+	}
+	/* the groups' sums, then one row per CTA */
+#pragma unroll
+	for (int b = 0; b < TL::NB; b++)
+		if (TL::live(tid, b))
+#pragma unroll
+			for (int q = 0; q < R; q++)
+				pk[tid + b * C::T + q * NBF] = acc[b][q];
+	__syncthreads();
+	float2 *row = a.partials + (size_t)blockIdx.x * L;
+	for (int i = threadIdx.x; i < L; i += blockDim.x) {
+		float2 sum = park[i];
+#pragma unroll
+		for (int gg = 1; gg < C::G; gg++)
+			sum = cadd(sum, park[(size_t)gg * L + i]);
+		row[i] = sum;
+	}
+}
+
+template <class C> constexpr size_t kgrad_smem_bytes()
+{
+	return Layout<C, FGK_OP_FORWARD>::DIRECT_BYTES + sizeof(float2) * (size_t)C::G * C::L;
+}
+
 /* ------------------------------------------------------------------------
  * Registry entries */
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
+typedef void (*kgrad_fn)(const fgk_plan, KgradArgs);
 
 struct StaticEntry {
 	uint32_t  mod, L, T, G, n, tma;
 	uint32_t  radices[FGK_MAX_STAGES];
 	size_t    smem[FGK_OP_COUNT];
 	static_fn fn[FGK_OP_COUNT];
+	kgrad_fn  kgrad; /* the taps-gradient kernel of this configuration, or null */
+	size_t    kgrad_smem;
 };
 
 template <class C, int OP> constexpr size_t smem_bytes()
@@ -843,6 +954,17 @@ template <class C, int OPS> StaticEntry make_entry()
 		e.fn[FGK_OP_CORR] = kernel_of<C, FGK_OP_CORR>();
 		e.smem[FGK_OP_CORR] = smem_bytes<C, FGK_OP_CORR>();
 	}
+	return e;
+}
+
+/* adds the taps-gradient kernel to an entry (direct-load, in-place
+ * configurations: the kernel is built from their transform stages) */
+template <class C> StaticEntry with_kgrad(StaticEntry e)
+{
+	static_assert(C::MODE == 0, "the gradient kernel uses the in-place stages");
+	static_assert(kgrad_smem_bytes<C>() <= FGK_SMEM_LIMIT, "gradient kernel exceeds shared memory");
+	e.kgrad = static_kernel_kgrad<C>;
+	e.kgrad_smem = kgrad_smem_bytes<C>();
 	return e;
 }
 

@@ -12,7 +12,8 @@
  * Unlike the 1536-bin kernels, fewer twiddle reads do not pay here: at
  * 4096 bins a thread runs one radix-16 butterfly per stage with all 256
  * threads busy, and the extra multiplies lengthen it. The chain is a
- * palindrome, so its twiddles are staged once. */
+ * palindrome, so its twiddles are staged once. V0 also carries the
+ * taps-gradient kernel of the adjoint (static_kernel_kgrad). */
 #include "fgk_static.cuh"
 
 namespace fgk {
@@ -29,7 +30,7 @@ int static_entries_4096(const StaticEntry **out)
 	static StaticEntry t[7];
 	static bool init = false;
 	if (!init) {
-		t[0] = make_entry<V0, OPS_ALL>();
+		t[0] = with_kgrad<V0>(make_entry<V0, OPS_ALL>());
 		t[1] = make_entry<V1, OPS_ALL>();
 		t[2] = make_entry<V2, OPS_CONV_CORR>();
 		t[3] = make_entry<V3, OPS_CONV_CORR>();
