@@ -13,6 +13,11 @@ Writes
                        each bin) for every size in 2..4096 with a plan, both
                        modulations, SIMD widths 1, 4 and 8, plus a sha256 of the
                        layout for every 2^a 3^b 5^{0,1} size in 4097..65536.
+  ref_layouts_beyond.npz  the same sha256 for the sizes beyond 65536 bins
+                       that the GPU tests run (two- and three-level splits):
+                       131072, 393216 and 15,728,640 bins.
+
+    python tests/golden/make_golden.py --beyond   (only ref_layouts_beyond.npz)
 The layout is read off the reference itself: a kernel input whose
 modulated sequence is a unit impulse at index 1 has spectrum
 W[k] = e^{-j 2 pi k / L}, so the phase of each kernel-buffer slot names its bin.
@@ -66,7 +71,51 @@ def layout_hash(off: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(off, np.int64).tobytes()).hexdigest()
 
 
+BEYOND = [131072, 393216, 15728640]
+
+
+def layout_from_reference_fast(R: O.Reference, mod: int, L: int, V: int) -> np.ndarray:
+    """layout_from_reference, vectorised for large L: the same impulse, the
+    same reading of each slot's phase as its bin, and the same check that
+    the slots form a permutation of the bins (at 15,728,640 bins the bins
+    are 4e-7 rad apart, well above the float32 phase error of the slots)."""
+    h = np.zeros(2 * L, np.float64)
+    if mod == O.MOD_COMPLEX:
+        h[2] = 1.0
+    else:
+        a = np.pi / (2.0 * L)
+        h[1] = np.cos(a)
+        h[L + 1] = -np.sin(a)
+    K = R.get_kernel(mod, L, h.astype(np.float32)).astype(np.float64).reshape(L // V, 2, V)
+    slot_re = (2 * V * np.arange(L // V)[:, None] + np.arange(V)[None, :]).ravel()
+    k = np.rint(-np.arctan2(K[:, 1, :].ravel(), K[:, 0, :].ravel()) * L / (2 * np.pi)).astype(np.int64) % L
+    assert np.all(np.bincount(k, minlength=L) == 1), (mod, L, V)
+    off = np.empty(L, np.int64)
+    off[k] = slot_re
+    return off
+
+
+def beyond(refs):
+    rows = []
+    for vw in (1, 4, 8):
+        for mod in (O.MOD_COMPLEX, O.MOD_FREQ_OFFSET_REAL):
+            for L in BEYOND:
+                V = O.port().oracle_lane_width(mod, L, vw)
+                off = layout_from_reference_fast(refs[vw], mod, L, V)
+                rows.append((vw, mod, L, V, layout_hash(off)))
+    np.savez_compressed(os.path.join(HERE, "ref_layouts_beyond.npz"),
+                        vw=np.array([r[0] for r in rows], np.int64), mod=np.array([r[1] for r in rows], np.int64),
+                        L=np.array([r[2] for r in rows], np.int64), V=np.array([r[3] for r in rows], np.int64),
+                        sha256=np.array([r[4] for r in rows]))
+    print("wrote", len(rows), "layout hashes beyond 65536 bins")
+
+
 def main():
+    if "--beyond" in sys.argv:
+        if not O.build_reference():
+            raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
+        beyond({vw: O.Reference(vw) for vw in (1, 4, 8)})
+        return
     if not O.build_reference():
         raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
     refs = {vw: O.Reference(vw) for vw in (1, 4, 8)}

@@ -10,7 +10,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import GOLDEN, ROOT
 
 HEADERS = [os.path.join(ROOT, "include", h) for h in sorted(os.listdir(os.path.join(ROOT, "include"))) if h.endswith(".h")]
 
@@ -51,6 +51,18 @@ def test_layout_matches_reference_small(fftset_lib, golden_layouts):
 def test_layout_matches_reference_large(fftset_lib, golden_layouts):
     g = golden_layouts
     for vw, mod, L, V, sha in zip(g["large_vw"], g["large_mod"], g["large_L"], g["large_V"], g["large_sha256"]):
+        off, lanes = fftset_lib.kernel_layout(int(mod), int(L), int(vw))
+        assert lanes == V
+        assert hashlib.sha256(np.asarray(off, np.int64).tobytes()).hexdigest() == sha, (vw, mod, L)
+
+
+def test_layout_matches_reference_beyond_65536(fftset_lib):
+    """Sizes of two- and three-level splits (131072, 393216, 15,728,640 bins):
+    layouts read off the reference itself (tests/golden/make_golden.py
+    --beyond), widths 1, 4 and 8, both modulations."""
+    g = np.load(os.path.join(GOLDEN, "ref_layouts_beyond.npz"))
+    assert len(g["L"]) == 18
+    for vw, mod, L, V, sha in zip(g["vw"], g["mod"], g["L"], g["V"], g["sha256"]):
         off, lanes = fftset_lib.kernel_layout(int(mod), int(L), int(vw))
         assert lanes == V
         assert hashlib.sha256(np.asarray(off, np.int64).tobytes()).hexdigest() == sha, (vw, mod, L)

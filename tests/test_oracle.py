@@ -8,6 +8,7 @@ import os
 import numpy as np
 import pytest
 
+from conftest import GOLDEN
 from oracle import oracle as O
 
 CASES = [(m, L) for m in (0, 1) for L in O.REFERENCE_TEST_LENGTHS] + [(0, 1024), (1, 1536), (1, 4096)]
@@ -59,6 +60,14 @@ def test_oracle_layout_matches_reference(golden_layouts, vw):
 def test_oracle_layout_hashes_large(golden_layouts):
     g = golden_layouts
     for vw, mod, L, V, sha in zip(g["large_vw"], g["large_mod"], g["large_L"], g["large_V"], g["large_sha256"]):
+        off, v = O.kernel_offsets(int(mod), int(L), int(vw))
+        assert v == V
+        assert hashlib.sha256(np.ascontiguousarray(off, np.int64).tobytes()).hexdigest() == sha, (vw, mod, L)
+
+
+def test_oracle_layout_hashes_beyond_65536():
+    g = np.load(os.path.join(GOLDEN, "ref_layouts_beyond.npz"))
+    for vw, mod, L, V, sha in zip(g["vw"], g["mod"], g["L"], g["V"], g["sha256"]):
         off, v = O.kernel_offsets(int(mod), int(L), int(vw))
         assert v == V
         assert hashlib.sha256(np.ascontiguousarray(off, np.int64).tobytes()).hexdigest() == sha, (vw, mod, L)
