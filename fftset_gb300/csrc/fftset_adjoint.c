@@ -53,7 +53,8 @@ static int fsa_rc(struct fs_impl *fs, int rc)
  * FREQ_OFFSET_REAL forward layout (or natural order), then the inverse.
  * Returns -FFTSET_E_UNSUPPORTED when the size has no such kernel. */
 static int fsa_taps_fused(const struct fftset_fft *f, float *grad_taps, const float *g, size_t g_stride,
-                          const float *x, size_t x_stride, unsigned count)
+                          const float *x, size_t x_stride, unsigned count, float *grad_input, size_t gi_stride,
+                          const float *kern)
 {
 	struct fs_impl *fs = f->fs;
 	const size_t L = f->lfft, nf = 2 * L;
@@ -68,8 +69,14 @@ static int fsa_taps_fused(const struct fftset_fft *f, float *grad_taps, const fl
 		return -rc;
 	partials = (float *)fs->stage[FSA_SLOT];
 	S = partials + (size_t)cap * nf;
-	if ((rc = fgk_launch_static_kgrad(&f->vp[v], v, g, g_stride, x, x_stride, count, partials, cap, &rows, fs->stream,
-	                                  fs->num_sms)) != 0)
+	if (grad_input)
+		/* both gradients in one pass: g_b is transformed once for both */
+		rc = fgk_launch_static_adj(&f->vp[v], v, g, g_stride, x, x_stride, grad_input, gi_stride, kern, count,
+		                           partials, cap, &rows, fs->stream, fs->num_sms);
+	else
+		rc = fgk_launch_static_kgrad(&f->vp[v], v, g, g_stride, x, x_stride, count, partials, cap, &rows, fs->stream,
+		                             fs->num_sms);
+	if (rc != 0)
 		return rc < 0 ? -FFTSET_E_UNSUPPORTED : rc;
 	if ((rc = fgk_launch_kgrad_reduce(partials, rows, (uint32_t)L, f->modulator->freq_offset_real, S, fs->stream)) !=
 	    0)
@@ -163,17 +170,26 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
 
 	FS_RANGE_PUSH("fftset_fft_conv_adjoint_batch");
 	pthread_mutex_lock(&fs->lock); /* the adjoint's scratch slot */
-	if (grad_input) {
-		rc = fs_launch(fft, FGK_OP_CORR, grad_input, grad_output, kernel_buf, count, go_stride, gi_stride);
-		if ((rc = fsa_rc(fs, rc)) != 0)
+	rc = -FFTSET_E_UNSUPPORTED;
+	if (grad_taps) {
+		/* the compiled one-pass kernels where the size has them (both
+		 * gradients, or the taps gradient alone) */
+		rc = fsa_taps_fused(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count, grad_input,
+		                    gi_stride, kernel_buf);
+		if (rc != -FFTSET_E_UNSUPPORTED && (rc = fsa_rc(fs, rc)) != 0)
 			goto done;
 	}
-	if (grad_taps) {
-		rc = fsa_taps_fused(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
-		if (rc == -FFTSET_E_UNSUPPORTED)
+	if (rc == -FFTSET_E_UNSUPPORTED || (!grad_taps && grad_input)) {
+		if (grad_input) {
+			rc = fs_launch(fft, FGK_OP_CORR, grad_input, grad_output, kernel_buf, count, go_stride, gi_stride);
+			if ((rc = fsa_rc(fs, rc)) != 0)
+				goto done;
+		}
+		if (grad_taps) {
 			rc = fsa_taps(fft, grad_taps, grad_output, go_stride, input_buf, in_stride, count);
-		if ((rc = fsa_rc(fs, rc)) != 0)
-			goto done;
+			if ((rc = fsa_rc(fs, rc)) != 0)
+				goto done;
+		}
 	}
 	if (fs->blocking) {
 		if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) == 0)

@@ -223,6 +223,12 @@ int fgk_static_kgrad_variant(uint32_t modulation, uint32_t L);
 int fgk_launch_static_kgrad(const fgk_plan *p, int v, const float *g, size_t g_stride, const float *x,
                             size_t x_stride, uint32_t count, float *partials, uint32_t max_rows, uint32_t *rows,
                             void *stream, int num_sms);
+/* The one-pass adjoint of the same variant (static_kernel_adj): writes dx
+ * (the correlation of each g_b with the taps, as FGK_OP_CORR) and the same
+ * partial rows as the taps-gradient kernel. */
+int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, size_t g_stride, const float *x,
+                          size_t x_stride, float *dx, size_t dx_stride, const float *kern, uint32_t count,
+                          float *partials, uint32_t max_rows, uint32_t *rows, void *stream, int num_sms);
 
 #ifdef __cplusplus
 }

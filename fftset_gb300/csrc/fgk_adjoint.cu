@@ -41,15 +41,30 @@ __global__ void kg_spec_partial(const float2 *__restrict__ S, const float2 *__re
 }
 
 /* out = sum over the P partials, in natural order (pack == 0) or in the
- * FREQ_OFFSET_REAL forward layout from packed-sequence bins (pack == 1) */
-__global__ void kg_reduce(const float2 *__restrict__ partials, uint32_t P, uint32_t L, int pack, float2 *out)
+ * FREQ_OFFSET_REAL forward layout from packed-sequence bins (pack == 1).
+ * A CTA covers KG_BINS bins with KG_SPLIT threads per bin, each summing every
+ * KG_SPLIT-th partial (independent loads in flight), then the KG_SPLIT sums
+ * of a bin are added in shared memory in a fixed order. */
+constexpr int KG_BINS = 32, KG_SPLIT = 8;
+__global__ void __launch_bounds__(KG_BINS *KG_SPLIT) kg_reduce(const float2 *__restrict__ partials, uint32_t P,
+                                                              uint32_t L, int pack, float2 *out)
 {
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= L)
-		return;
+	__shared__ float2 part[KG_SPLIT][KG_BINS];
+	const uint32_t lane = threadIdx.x % KG_BINS, r0 = threadIdx.x / KG_BINS;
+	const uint32_t i = blockIdx.x * KG_BINS + lane;
 	float2 a = make_float2(0.f, 0.f);
-	for (uint32_t p = 0; p < P; p++)
-		a = cadd(a, partials[(uint64_t)p * L + i]);
+	if (i < L) {
+#pragma unroll 4
+		for (uint32_t p = r0; p < P; p += KG_SPLIT)
+			a = cadd(a, __ldcg(partials + (uint64_t)p * L + i));
+	}
+	part[r0][lane] = a;
+	__syncthreads();
+	if (r0 != 0 || i >= L)
+		return;
+#pragma unroll
+	for (int r = 1; r < KG_SPLIT; r++)
+		a = cadd(a, part[r][lane]);
 	if (!pack)
 		out[i] = a;
 	else if (i < ((L + 1) >> 1))
@@ -77,8 +92,8 @@ extern "C" int fgk_launch_kgrad_reduce(const float *partials, uint32_t P, uint32
                                        void *stream)
 {
 	using namespace fgk;
-	kg_reduce<<<(L + 63) / 64, 64, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2 *>(partials), P, L, pack,
-	                                                          reinterpret_cast<float2 *>(out));
+	kg_reduce<<<(L + KG_BINS - 1) / KG_BINS, KG_BINS * KG_SPLIT, 0, (cudaStream_t)stream>>>(
+	    reinterpret_cast<const float2 *>(partials), P, L, pack, reinterpret_cast<float2 *>(out));
 	fgk_count_launch();
 	return (int)cudaGetLastError();
 }

@@ -168,3 +168,34 @@ extern "C" int fgk_launch_static_kgrad(const fgk_plan *p, int v, const float *g,
 	*rows = (uint32_t)grid;
 	return (int)cudaGetLastError();
 }
+
+extern "C" int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, size_t g_stride, const float *x,
+                                     size_t x_stride, float *dx, size_t dx_stride, const float *kern, uint32_t count,
+                                     float *partials, uint32_t max_rows, uint32_t *rows, void *stream, int num_sms)
+{
+	using namespace fgk;
+	const StaticEntry *e;
+	const int nv = variants(p->modulation, p->L, &e);
+	if (v < 0 || v >= nv || !e[v].adj)
+		return -1;
+	e += v;
+	int per_sm = 0;
+	cudaError_t err = launch_setup((const void *)e->adj, (int)(e->T * e->G), e->adj_smem, &per_sm);
+	if (err != cudaSuccess)
+		return (int)err;
+	if (per_sm < 1)
+		return (int)cudaErrorInvalidConfiguration;
+	uint64_t grid = (uint64_t)per_sm * (uint64_t)num_sms;
+	const uint64_t need = ((uint64_t)count + e->G - 1) / e->G;
+	if (grid > need)
+		grid = need;
+	if (grid > max_rows)
+		grid = max_rows;
+	if (grid == 0)
+		return (int)cudaErrorInvalidValue;
+	AdjArgs a{g, x, kern, dx, g_stride, x_stride, dx_stride, count, reinterpret_cast<float2 *>(partials)};
+	e->adj<<<(unsigned)grid, e->T * e->G, e->adj_smem, (cudaStream_t)stream>>>(*p, a);
+	fgk_count_launch();
+	*rows = (uint32_t)grid;
+	return (int)cudaGetLastError();
+}

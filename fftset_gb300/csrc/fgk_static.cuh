@@ -891,10 +891,188 @@ template <class C> constexpr size_t kgrad_smem_bytes()
 	return Layout<C, FGK_OP_FORWARD>::DIRECT_BYTES + sizeof(float2) * (size_t)C::G * C::L;
 }
 
+/* ---- the adjoint in one pass ---------------------------------------------
+ * For block pairs (g_b, x_b): dx_b, the correlation of g_b with the taps
+ * (the convolution of g_b with the conjugated kernel spectrum, what
+ * FGK_OP_CORR computes), and the CTA's sum of W_g conj(W_x) for the taps
+ * gradient. g_b is transformed once for both: its spectrum is parked on its
+ * way through the correlation, then x_b is transformed and the product
+ * accumulated. Per block pair HBM sees one read of g_b and x_b and one write
+ * of dx_b. The FREQ_OFFSET_REAL modulation of the first and last stages is
+ * mods[j] e^{-j pi p/(2R)} (mod_steps) for the points j + p L/R of butterfly
+ * j, so only L/R table entries are staged, which leaves shared memory for
+ * the park buffers. */
+struct AdjArgs {
+	const float *g, *x, *kern;
+	float       *dx;
+	size_t       g_stride, x_stride, dx_stride;
+	uint32_t     count;
+	float2      *partials; /* gridDim.x rows of L */
+};
+
+template <class C> struct AdjLayout {
+	static constexpr int MODS = C::MOD == FGK_MOD_FREQOFF ? C::L / C::fr(0) : 0; /* float2 */
+	static constexpr size_t TW = C::TWG ? 0 : (size_t)C::TW_TOTAL;
+	static constexpr size_t BYTES =
+	    sizeof(float2) * (TW + MODS + (size_t)C::L + (size_t)C::G * C::SLOTS + (size_t)C::G * C::L);
+};
+
+/* stage 0 of a forward chain from HBM into the exchange buffer */
+template <class C>
+__device__ __forceinline__ void adj_first(int tid, int g, const Ex<C> &ex, const float *x, const float2 *mods,
+                                          const float2 *tws)
+{
+	constexpr int L = C::L, R = C::fr(0), NBF = L / R;
+	using T0 = Tile<C, R>;
+	T0 t0;
+	if constexpr (C::MOD == FGK_MOD_FREQOFF) {
+#pragma unroll
+		for (int b = 0; b < T0::NB; b++) {
+			const int j = tid + b * C::T;
+			if (T0::live(tid, b)) {
+#pragma unroll
+				for (int p = 0; p < R; p++)
+					t0.v[b][p] = make_float2(ldcs(x + j + p * NBF), -ldcs(x + L + j + p * NBF));
+				mod_steps<R>(t0.v[b], mods[j]);
+			}
+		}
+	} else {
+		t0.load(tid, [&](int i) { return ldcs2(reinterpret_cast<const float2 *>(x) + i); });
+	}
+	t0.template butterfly<1>(tid, tws);
+	t0.template store<1>(tid, [&](int i, float2 v) { ex.put(i, v); });
+	gsync<C>(g);
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_adj(const fgk_plan p, AdjArgs a)
+{
+	extern __shared__ float2 smem[];
+	using Lay = AdjLayout<C>;
+	constexpr int L = C::L, N = C::N;
+	constexpr int R = C::fr(N - 1), NS = C::fns(N - 1), NBF = L / R;       /* last forward stage */
+	constexpr int RL = C::ir(N - 1), NSL = C::ins(N - 1), NBFL = L / RL; /* last reversed stage */
+	constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
+	static_assert(N >= 2, "the adjoint kernel needs two or more stages");
+	using TL = Tile<C, R>;
+	using TR = Tile<C, RL>;
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *exb = ks + L;
+	float2 *park = exb + (size_t)C::G * C::SLOTS;
+	if constexpr (!C::TWG)
+		stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
+	if constexpr (FREQ)
+		for (int i = threadIdx.x; i < Lay::MODS; i += blockDim.x)
+			mods[i] = __ldg((const float2 *)p.modtw + i);
+	for (int i = threadIdx.x; i < L; i += blockDim.x) {
+		const int o = __ldg(p.kidx + i);
+		ks[i] = make_float2(__ldg(a.kern + o), -__ldg(a.kern + o + (int)p.kvw)); /* conj K: correlation */
+	}
+	__syncthreads();
+
+	const int g = threadIdx.x / C::T;
+	const int tid = C::wt((int)threadIdx.x - g * C::T, g);
+	const Ex<C> ex{exb + (size_t)g * C::SLOTS};
+	auto exput = [&](int i, float2 v) { ex.put(i, v); };
+	float2 *pk = park + (size_t)g * L;
+	float2 acc[TL::NB][R];
+#pragma unroll
+	for (int b = 0; b < TL::NB; b++)
+#pragma unroll
+		for (int q = 0; q < R; q++)
+			acc[b][q] = make_float2(0.f, 0.f);
+	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.count; t += (uint64_t)gridDim.x * C::G) {
+		/* g_b: forward chain, park W_g, product with conj K, reversed chain */
+		adj_first<C>(tid, g, ex, a.g + t * a.g_stride, mods, tws);
+		fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
+		{
+			TL tt;
+			tt.load(tid, ex);
+			gsync<C>(g);
+			tt.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
+#pragma unroll
+			for (int b = 0; b < TL::NB; b++) {
+				const int j = tid + b * C::T;
+				if (TL::live(tid, b)) {
+#pragma unroll
+					for (int q = 0; q < R; q++) {
+						pk[j + q * NBF] = tt.v[b][q];
+						tt.v[b][q] = conjf2(cmul(tt.v[b][q], ks[j + q * NBF]));
+					}
+					Radix<R>::run(tt.v[b]);
+				}
+			}
+			tt.template store<1>(tid, exput);
+			gsync<C>(g);
+		}
+		inv_mid<C, 1, N - 1>(tid, g, ex, tws);
+		{
+			float *y = a.dx + t * a.dx_stride;
+			TR tt;
+			tt.load(tid, ex);
+			tt.template butterfly<NSL>(tid, tws + C::itw_off(N - 1));
+#pragma unroll
+			for (int b = 0; b < TR::NB; b++) {
+				const int j = tid + b * C::T;
+				if (TR::live(tid, b)) {
+					if constexpr (FREQ) {
+						mod_steps<RL>(tt.v[b], mods[j]);
+#pragma unroll
+						for (int q = 0; q < RL; q++) {
+							stcs(y + j + q * NBFL, tt.v[b][q].x);
+							stcs(y + L + j + q * NBFL, tt.v[b][q].y);
+						}
+					} else {
+#pragma unroll
+						for (int q = 0; q < RL; q++)
+							stcs2(reinterpret_cast<float2 *>(y) + j + q * NBFL, conjf2(tt.v[b][q]));
+					}
+				}
+			}
+			gsync<C>(g);
+		}
+		/* x_b: forward chain, product with the parked W_g */
+		adj_first<C>(tid, g, ex, a.x + t * a.x_stride, mods, tws);
+		fwd_mid<C, 1, N - 1>(tid, g, ex, tws);
+		{
+			TL tx;
+			tx.load(tid, ex);
+			gsync<C>(g);
+			tx.template butterfly<NS>(tid, tws + C::ftw_off(N - 1));
+#pragma unroll
+			for (int b = 0; b < TL::NB; b++)
+				if (TL::live(tid, b))
+#pragma unroll
+					for (int q = 0; q < R; q++) {
+						const int i = tid + b * C::T + q * NBF;
+						acc[b][q] = cadd(acc[b][q], cmulc(pk[i], tx.v[b][q]));
+					}
+		}
+	}
+#pragma unroll
+	for (int b = 0; b < TL::NB; b++)
+		if (TL::live(tid, b))
+#pragma unroll
+			for (int q = 0; q < R; q++)
+				pk[tid + b * C::T + q * NBF] = acc[b][q];
+	__syncthreads();
+	float2 *row = a.partials + (size_t)blockIdx.x * L;
+	for (int i = threadIdx.x; i < L; i += blockDim.x) {
+		float2 sum = park[i];
+#pragma unroll
+		for (int gg = 1; gg < C::G; gg++)
+			sum = cadd(sum, park[(size_t)gg * L + i]);
+		row[i] = sum;
+	}
+}
+
 /* ------------------------------------------------------------------------
  * Registry entries */
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
 typedef void (*kgrad_fn)(const fgk_plan, KgradArgs);
+typedef void (*adj_fn)(const fgk_plan, AdjArgs);
 
 struct StaticEntry {
 	uint32_t  mod, L, T, G, n, tma;
@@ -903,6 +1081,8 @@ struct StaticEntry {
 	static_fn fn[FGK_OP_COUNT];
 	kgrad_fn  kgrad; /* the taps-gradient kernel of this configuration, or null */
 	size_t    kgrad_smem;
+	adj_fn    adj; /* the one-pass adjoint (input and taps gradients), or null */
+	size_t    adj_smem;
 };
 
 template <class C, int OP> constexpr size_t smem_bytes()
@@ -957,14 +1137,18 @@ template <class C, int OPS> StaticEntry make_entry()
 	return e;
 }
 
-/* adds the taps-gradient kernel to an entry (direct-load, in-place
- * configurations: the kernel is built from their transform stages) */
+/* adds the taps-gradient and one-pass adjoint kernels to an entry
+ * (direct-load, in-place configurations: the kernels are built from their
+ * transform stages) */
 template <class C> StaticEntry with_kgrad(StaticEntry e)
 {
 	static_assert(C::MODE == 0, "the gradient kernel uses the in-place stages");
 	static_assert(kgrad_smem_bytes<C>() <= FGK_SMEM_LIMIT, "gradient kernel exceeds shared memory");
+	static_assert(AdjLayout<C>::BYTES <= FGK_SMEM_LIMIT, "adjoint kernel exceeds shared memory");
 	e.kgrad = static_kernel_kgrad<C>;
 	e.kgrad_smem = kgrad_smem_bytes<C>();
+	e.adj = static_kernel_adj<C>;
+	e.adj_smem = AdjLayout<C>::BYTES;
 	return e;
 }
 

@@ -710,6 +710,7 @@ int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fg
 	task_kernel<inverse, freq, THREADS, MINB><<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
 	                                                              hcounters, scratch, in_base, out_base, err,
 	                                                              spin_limit);
+	fgk_count_launch();
 	return (int)cudaGetLastError();
 }
 

@@ -65,10 +65,13 @@ def test_adjoint_against_fp64(gpu_set, mod, L):
     assert O.rel_l2(dh, wh) <= tol(mod, L)
 
 
-def test_adjoint_strides_and_single_outputs(gpu_set):
-    """Padded rows, one output at a time, count 1 and count 0."""
+@pytest.mark.parametrize("L", [1536, 4096])
+def test_adjoint_strides_and_single_outputs(gpu_set, L):
+    """Padded rows, one output at a time, both at once, count 1 and count 0.
+    At 4096 bins the compiled one-pass kernels run (both gradients, or the
+    taps gradient alone); at 1536 bins the batched-forward route."""
     import torch
-    L, B, pad = 1536, 7, 10
+    B, pad = 7, 10
     f = gpu_set.create_fft(1, L)
     rng = np.random.default_rng(11)
     xs = rng.standard_normal((B, 2 * L + pad)).astype(np.float32)
@@ -84,6 +87,11 @@ def test_adjoint_strides_and_single_outputs(gpu_set):
     dh = torch.empty(2 * L, device="cuda")
     f.conv_adjoint_batch(None, dh, dev(gs), dev(xs), K)
     assert O.rel_l2(host(dh), wh) <= tol(1, L)
+    dx2, dh2 = torch.zeros(B, 2 * L + 4, device="cuda"), torch.empty(2 * L, device="cuda")
+    f.conv_adjoint_batch(dx2, dh2, dev(gs), dev(xs), K)
+    assert O.rel_l2(host(dx2)[:, :2 * L], wx) <= tol(1, L)
+    assert np.all(host(dx2)[:, 2 * L:] == 0)
+    assert O.rel_l2(host(dh2), wh) <= tol(1, L)
     one_dx, one_dh = torch.empty(2 * L, device="cuda"), torch.empty(2 * L, device="cuda")
     f.conv_adjoint_batch(one_dx, one_dh, dev(gs[0, :2 * L]), dev(xs[0, :2 * L]), K)
     w1x, w1h = O.conv_adjoint64(1, xs[:1, :2 * L], h, gs[:1, :2 * L])
