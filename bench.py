@@ -706,14 +706,26 @@ def profile_kernels(torch, fs):
     run("adjoint dL/dtaps FREQ 4096 x2048", lambda: g.conv_adjoint_batch(None, dh, w, x, K), 2 * B * nf * 4 + 4 * nf,
         3)
     del x, w, dx
-    # two-pass kernels: convolution beyond the shared-memory limit
+    # beyond the shared-memory limit: the convolution (two task launches),
+    # forward and inverse (one each); the two-pass kernels serve the
+    # fixed-scratch entry point
     h = S.create_fft(fs.FREQ_OFFSET_REAL, 65536)
     B, nf = 512, 131072
     x, y = buf(B * nf).view(B, nf), torch.empty(B, nf, device="cuda")
     K = torch.empty(nf, device="cuda")
     h.conv_get_kernel(K, buf(nf))
-    run("fourstep conv FREQ 65536 x512 (pass 1, 2 of the forward; pass 1, 2 of the inverse)",
-        lambda: h.conv_batch(y, x, K), 2 * B * nf * 4 + 4 * nf, 4)
+    run("task_kernel conv FREQ 65536 x512 (forward with the spectrum product, then inverse)",
+        lambda: h.conv_batch(y, x, K), 2 * B * nf * 4 + 4 * nf, 2)
+    run("fourstep get_kernel FREQ 65536 x512 (pass 1, pass 2)", lambda: h.conv_get_kernel_batch(y, x),
+        2 * B * nf * 4, 2)
+    fixed = fs.library().fftset_fft_execute_fixed_scratch
+    fixed.restype = ctypes.c_int
+    fixed.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint]
+    nfix = (8 << 20) // nf  # the fixed array's limit: 64 blocks
+    run(f"fourstep conv FREQ 65536 x{nfix}, fixed-scratch entry point (pass 1, 2 of the forward; of the inverse)",
+        lambda: fixed(h.handle, fs.OP_CONV, y.data_ptr(), nf, x.data_ptr(), nf, K.data_ptr(), nfix),
+        2 * nfix * nf * 4 + 4 * nf, 4)
     run("task_kernel forward FREQ 65536 x512 (two-level)", lambda: h.forward_batch(y, x), 2 * B * nf * 4, 1)
     run("task_kernel inverse FREQ 65536 x512 (two-level)", lambda: h.inverse_batch(y, x), 2 * B * nf * 4, 1)
     del x, y

@@ -745,9 +745,28 @@ static int fs_launch_fourstep(const struct fftset_fft *f, int op, float *out, co
 	const size_t nf = 2 * (size_t)f->lfft;
 	int rc = -FFTSET_E_UNSUPPORTED;
 	pthread_mutex_lock(&fs->lock);
-	if (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE)
+	if (op == FGK_OP_FORWARD || op == FGK_OP_INVERSE) {
 		/* tile tasks (fgk_tasks.cuh): two- or three-level split */
-		rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, fs->stream);
+		rc = fs_tasks_batch((struct fftset_fft *)f, op, out, out_stride, in, in_stride, count, fs->stream, NULL);
+	} else if (op == FGK_OP_CONV || op == FGK_OP_CORR) {
+		/* the forward task launch with the spectrum product fused into its
+		 * final stores, into the work buffer (natural bins, the forward's
+		 * output layout), then the inverse task launch from it: the
+		 * convolution theorem in the library's own transforms, inverse(
+		 * forward(x) K) = complex_bins x the (negacyclic or cyclic)
+		 * convolution, two launches through HBM */
+		const fgk_product prod = {kern, f->kidx4, (int32_t)f->lanes, op == FGK_OP_CORR};
+		const size_t is = count > 1 ? in_stride : nf, os = count > 1 ? out_stride : nf;
+		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0) {
+			rc = -rc;
+		} else {
+			float *work = (float *)fs->stage[3];
+			rc = fs_tasks_batch((struct fftset_fft *)f, FGK_OP_FORWARD, work, nf, in, is, count, fs->stream, &prod);
+			if (rc == 0)
+				rc = fs_tasks_batch((struct fftset_fft *)f, FGK_OP_INVERSE, out, os, work, nf, count, fs->stream,
+				                    NULL);
+		}
+	}
 	if (rc == -FFTSET_E_UNSUPPORTED) {
 		/* two passes through a work buffer of 2L floats per transform (the
 		 * library's own scratch: work_buf of the reference API may be host

@@ -115,9 +115,10 @@ int  fs_plan_error(void);
 /* forward / inverse of `count` device blocks of a four-step plan as one task
  * launch (fftset_ragged.c); returns 0, a negative FFTSET_E_* code or a
  * positive cudaError_t; FFTSET_E_UNSUPPORTED when the size has no tile split.
- * Called with fs->lock held. */
+ * prod (forward only, may be NULL): a spectrum product fused into the final
+ * stores. Called with fs->lock held. */
 int  fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
-                    unsigned count, cudaStream_t stream);
+                    unsigned count, cudaStream_t stream, const fgk_product *prod);
 void fsr_free(struct fftset_ragged *rb);
 /* applies a saved task-kernel schedule to a plan (fftset_ragged.c) */
 int  fsr_apply_schedule(struct fs_impl *fs, struct fftset_fft *f, const uint32_t *rad, uint32_t n, uint32_t tg,

@@ -391,12 +391,19 @@ struct fftset_ragged *fftset_ragged_create(struct fftset *fc, const struct fftse
 
 /* the launch sequence of direction `op`, on `s` (a task list does not
  * depend on the direction) */
-static int fsr_record(struct fftset_ragged *rb, int op, float *out, const float *in, cudaStream_t s)
+static int fsr_record_product(struct fftset_ragged *rb, int op, float *out, const float *in, cudaStream_t s,
+                              const fgk_product *prod)
 {
 	struct fs_impl *fs = rb->fs;
+	const fgk_product none = {NULL, NULL, 0, 0};
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
 	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, op, rb->modulation, in, out,
-	                        fs->num_sms, rb->wide, fs->dev_flag, fs->spin_limit, s);
+	                        fs->num_sms, rb->wide, fs->dev_flag, fs->spin_limit, prod ? *prod : none, s);
+}
+
+static int fsr_record(struct fftset_ragged *rb, int op, float *out, const float *in, cudaStream_t s)
+{
+	return fsr_record_product(rb, op, out, in, s, NULL);
 }
 
 /* Test hook: removes the batch's tasks of one kind (FGK_TASK_*), so that
@@ -529,7 +536,7 @@ unsigned fftset_ragged_persistent_items(const struct fftset_ragged *rb)
  * this plan, and a list being replaced is freed only after the stream's
  * earlier launches, which may use it, have finished (fsr_free). */
 int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in, size_t in_stride,
-                   unsigned count, cudaStream_t stream)
+                   unsigned count, cudaStream_t stream, const fgk_product *prod)
 {
 	struct fs_impl *fs = f->fs;
 	const size_t nf = 2 * (size_t)f->lfft;
@@ -596,7 +603,7 @@ int fs_tasks_batch(struct fftset_fft *f, int op, float *out, size_t out_stride, 
 		t->op = key_op;
 	}
 	t->used = ++f->tl_clock;
-	return fsr_record(t->rb, op, out, in, stream);
+	return fsr_record_product(t->rb, op, out, in, stream, prod);
 }
 
 /* ------------------------------------------------------------------------

@@ -129,6 +129,19 @@ typedef struct fgk_task {
 	uint32_t b;    /* SMALL: items | threads per item << 16 */
 } fgk_task;
 
+/* A spectrum product fused into the final stores of a forward task launch
+ * (ROWS and C tiles): W[m] times the kernel spectrum's bin m, read from a
+ * kernel buffer through its layout table (re at kern[kidx[m]], im kvw
+ * floats later), conjugated when conj is set; kern == NULL: no product. The
+ * convolution of sizes beyond the shared-memory limit is this forward
+ * followed by the inverse task launch. */
+typedef struct fgk_product {
+	const float   *kern;
+	const int32_t *kidx;
+	int32_t        kvw;
+	int32_t        conj;
+} fgk_product;
+
 /* A three-level item: passes A, B, C through two scratch areas; B tiles
  * wait for every A tile of the item, C tiles for every B tile. */
 typedef struct fgk_huge {
@@ -191,7 +204,7 @@ int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_pl
                         const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                         const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev,
                         float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
-                        int num_sms, int wide, int *err_flag, uint32_t spin_limit, void *stream);
+                        int num_sms, int wide, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream);
 int    fgk_tasks_grid(int num_sms, int wide);
 int    fgk_tasks_threads(int wide);
 /* points of a tile (items up to this size run whole) and the shared-memory

@@ -37,7 +37,7 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                                 const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev, float *scratch_dev,
                                 int op, int modulation, const float *in_base, float *out_base, int num_sms,
-                                int wide, int *err_flag, uint32_t spin_limit, void *stream)
+                                int wide, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream)
 {
 	const bool inv = op == FGK_OP_INVERSE, freq = modulation == FGK_MOD_FREQOFF;
 	cudaStream_t s = (cudaStream_t)stream;
@@ -57,5 +57,5 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	                   : (inv ? (freq ? fgk_launch_tasks_if : fgk_launch_tasks_ic)
 	                          : (freq ? fgk_launch_tasks_ff : fgk_launch_tasks_fc));
 	return launch(grid, tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, huges_dev, counters_dev, hcounters, scratch,
-	              in_base, out_base, err_flag, spin_limit, s);
+	              in_base, out_base, err_flag, spin_limit, prod, s);
 }

@@ -305,6 +305,14 @@ __device__ __forceinline__ void tk_signal(int *ctr)
 	}
 }
 
+/* v times bin m of the product's kernel spectrum (or its conjugate) */
+__device__ __forceinline__ float2 tk_product(const fgk_product &pr, uint32_t m, float2 v)
+{
+	const int o = __ldg(pr.kidx + m);
+	const float2 k = make_float2(__ldg(pr.kern + o), __ldg(pr.kern + o + pr.kvw));
+	return pr.conj ? cmulc(v, k) : cmul(v, k);
+}
+
 /* ---- SMALL: whole items side by side ---------------------------------- */
 /* n items of one size, tg threads each (group g = threadIdx / tg), each
  * group's first stage reading its item and its last stage writing its
@@ -417,8 +425,8 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
  * into X[k1 + L1 k2] */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg, float *out_base, float2 *scratch,
-                                          const int *done, int *err, uint32_t spin_limit, float2 *smem, int *failed,
-                                          Pre &&pre)
+                                          const int *done, int *err, uint32_t spin_limit, const fgk_product &prod,
+                                          float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
 	const int L1 = (int)p->L1, L2 = (int)p->L2;
@@ -444,6 +452,8 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		const int k1 = k1base + lane;
 		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * (uint32_t)k2;
 		if (!inverse) {
+			if (prod.kern)
+				v = tk_product(prod, m, v);
 			if (!freq)
 				__stcs(o2 + m, v);
 			else if (m < ((L + 1) >> 1))
@@ -567,8 +577,8 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
  * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
-                                        const int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
-                                        Pre &&pre)
+                                        const int *done_b, int *err, uint32_t spin_limit, const fgk_product &prod,
+                                        float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
@@ -594,6 +604,8 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 		const int k3 = j + q * nbf;
 		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * ((uint32_t)k2 + (uint32_t)L2 * k3);
 		if (!inverse) {
+			if (prod.kern)
+				v = tk_product(prod, m, v);
 			if (!freq)
 				__stcs(o2 + m, v);
 			else if (m < ((L + 1) >> 1))
@@ -620,7 +632,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
                 const fgk_huge *__restrict__ huges, int *counters, int *hcounters, float2 *scratch,
-                const float *in_base, float *out_base, int *err, uint32_t spin_limit)
+                const float *in_base, float *out_base, int *err, uint32_t spin_limit, const fgk_product prod)
 {
 	extern __shared__ float2 smem[];
 	__shared__ uint32_t cur;
@@ -662,7 +674,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_ROWS)
 			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, spin_limit,
-			                         smem, &failed, pre);
+			                         prod, smem, &failed, pre);
 		else if (tk.kind == FGK_TASK_PA)
 			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_PB)
@@ -670,7 +682,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 			                       spin_limit, smem, &failed, pre);
 		else
 			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, spin_limit,
-			                       smem, &failed, pre);
+			                       prod, smem, &failed, pre);
 		if (threadIdx.x == 0) {
 			if (copying) {
 				asm volatile("cp.async.wait_all;" ::: "memory");
@@ -700,7 +712,7 @@ template <bool inverse, bool freq, int THREADS, int MINB>
 int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans,
                  const fgk_rg_item *items, const fgk_big *bigs, const fgk_huge *huges, int *counters,
                  int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, uint32_t spin_limit,
-                 cudaStream_t stream)
+                 fgk_product prod, cudaStream_t stream)
 {
 	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
 	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq, THREADS, MINB>,
@@ -709,7 +721,7 @@ int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fg
 		return (int)e;
 	task_kernel<inverse, freq, THREADS, MINB><<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
 	                                                              hcounters, scratch, in_base, out_base, err,
-	                                                              spin_limit);
+	                                                              spin_limit, prod);
 	fgk_count_launch();
 	return (int)cudaGetLastError();
 }
@@ -719,7 +731,7 @@ int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fg
 #define FGKT_LAUNCH_ARGS                                                                                 \
 	uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans, const fgk_rg_item *items,     \
 	    const fgk_big *bigs, const fgk_huge *huges, int *counters, int *hcounters, float2 *scratch,              \
-	    const float *in_base, float *out_base, int *err, uint32_t spin_limit, cudaStream_t stream
+	    const float *in_base, float *out_base, int *err, uint32_t spin_limit, fgk_product prod, cudaStream_t stream
 #define FGKT_LAUNCH_PASS                                                                                 \
 	grid, tasks, ntasks, plans, items, bigs, huges, counters, hcounters, scratch, in_base, out_base, err, spin_limit, \
-	    stream
+	    prod, stream
