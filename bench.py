@@ -418,6 +418,37 @@ def workload_adjoint(fs, torch, peak):
             "relL2_dx_vs_fp64": rel_dx, "relL2_dtaps_vs_fp64_64blocks": rel_dh, "tolerance": O.tolerance(N)}
 
 
+def workload_conv_large(fs, torch, peak):
+    """FREQ_OFFSET_REAL convolution beyond the shared-memory limit: 65536
+    bins (131072 reals per block), 512 blocks, Gaussian input, decaying
+    Gaussian kernel; the kernel spectrum gathered into natural order, the
+    forward task launch with the spectrum product, the inverse task launch."""
+    from oracle import oracle as O
+    L, B = 65536, 512
+    N = 2 * L
+    rng = np.random.default_rng(12)
+    x_np = rng.standard_normal((B, N)).astype(np.float32)
+    h_np = (rng.standard_normal(N) * np.exp(-np.arange(N) / 4000.0)).astype(np.float32)
+    x, h = torch.from_numpy(x_np).cuda(), torch.from_numpy(h_np).cuda()
+    S = fs.FftSet()
+    S.set_stream(torch.cuda.current_stream())
+    f = S.create_fft(fs.FREQ_OFFSET_REAL, L)
+    K = torch.empty_like(h)
+    f.conv_get_kernel(K, h)
+    y = torch.empty_like(x)
+    S.set_blocking(False)
+    f.conv_batch(y, x, K)
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, lambda: f.conv_batch(y, x, K), 10, torch.cuda.current_stream())
+    S.check()
+    rel = O.rel_l2(y[:4].cpu().numpy(), O.negacyclic_conv64(x_np[:4], h_np))
+    S.close()
+    nbytes = 2 * B * N * 4 + N * 4
+    return {"workload": "freqoffsetreal_conv_L65536_x512", "ms": ms, "gbs": nbytes / ms / 1e6,
+            "frac_of_peak": nbytes / ms / 1e6 / peak, "launches_per_call": 3,
+            "relL2_vs_fp64_4blocks": rel, "tolerance": O.tolerance(N)}
+
+
 def dist_setup(n_gpus):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -565,7 +596,8 @@ def run_gb300(args):
         if world == 1 and not args.skip_workloads:
             del x, y, xh, yh
             torch.cuda.empty_cache()
-            for fn in (workload_percall_complex1024, workload_ragged, workload_large, workload_adjoint):
+            for fn in (workload_percall_complex1024, workload_ragged, workload_large, workload_adjoint,
+                       workload_conv_large):
                 try:
                     r = fn(fs, torch, peak)
                     others[r.pop("workload")] = r
@@ -714,8 +746,8 @@ def profile_kernels(torch, fs):
     x, y = buf(B * nf).view(B, nf), torch.empty(B, nf, device="cuda")
     K = torch.empty(nf, device="cuda")
     h.conv_get_kernel(K, buf(nf))
-    run("task_kernel conv FREQ 65536 x512 (forward with the spectrum product, then inverse)",
-        lambda: h.conv_batch(y, x, K), 2 * B * nf * 4 + 4 * nf, 2)
+    run("task_kernel conv FREQ 65536 x512 (spectrum gather, forward with the product, inverse)",
+        lambda: h.conv_batch(y, x, K), 2 * B * nf * 4 + 4 * nf, 3)
     run("fourstep get_kernel FREQ 65536 x512 (pass 1, pass 2)", lambda: h.conv_get_kernel_batch(y, x),
         2 * B * nf * 4, 2)
     fixed = fs.library().fftset_fft_execute_fixed_scratch

@@ -755,13 +755,18 @@ static int fs_launch_fourstep(const struct fftset_fft *f, int op, float *out, co
 		 * convolution theorem in the library's own transforms, inverse(
 		 * forward(x) K) = complex_bins x the (negacyclic or cyclic)
 		 * convolution, two launches through HBM */
-		const fgk_product prod = {kern, f->kidx4, (int32_t)f->lanes, op == FGK_OP_CORR};
 		const size_t is = count > 1 ? in_stride : nf, os = count > 1 ? out_stride : nf;
-		if ((rc = fs_stage_reserve(fs, 3, nf * count * sizeof(float))) != 0) {
+		if ((rc = fs_stage_reserve(fs, 3, nf * ((size_t)count + 1) * sizeof(float))) != 0) {
 			rc = -rc;
 		} else {
-			float *work = (float *)fs->stage[3];
-			rc = fs_tasks_batch((struct fftset_fft *)f, FGK_OP_FORWARD, work, nf, in, is, count, fs->stream, &prod);
+			/* the work buffer, then the kernel spectrum in natural order */
+			float *work = (float *)fs->stage[3], *spec = work + nf * (size_t)count;
+			const fgk_product prod = {spec};
+			rc = fgk_launch_spectrum_natural(kern, f->kidx4, (int)f->lanes, f->lfft, op == FGK_OP_CORR, spec,
+			                                 fs->stream);
+			if (rc == 0)
+				rc = fs_tasks_batch((struct fftset_fft *)f, FGK_OP_FORWARD, work, nf, in, is, count, fs->stream,
+				                    &prod);
 			if (rc == 0)
 				rc = fs_tasks_batch((struct fftset_fft *)f, FGK_OP_INVERSE, out, os, work, nf, count, fs->stream,
 				                    NULL);

@@ -395,7 +395,7 @@ static int fsr_record_product(struct fftset_ragged *rb, int op, float *out, cons
                               const fgk_product *prod)
 {
 	struct fs_impl *fs = rb->fs;
-	const fgk_product none = {NULL, NULL, 0, 0};
+	const fgk_product none = {NULL};
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
 	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, op, rb->modulation, in, out,
 	                        fs->num_sms, rb->wide, fs->dev_flag, fs->spin_limit, prod ? *prod : none, s);

@@ -130,17 +130,19 @@ typedef struct fgk_task {
 } fgk_task;
 
 /* A spectrum product fused into the final stores of a forward task launch
- * (ROWS and C tiles): W[m] times the kernel spectrum's bin m, read from a
- * kernel buffer through its layout table (re at kern[kidx[m]], im kvw
- * floats later), conjugated when conj is set; kern == NULL: no product. The
+ * (ROWS and C tiles): W[m] times spec[m], the kernel spectrum in natural bin
+ * order (fgk_launch_spectrum_natural); spec == NULL: no product. The
  * convolution of sizes beyond the shared-memory limit is this forward
  * followed by the inverse task launch. */
 typedef struct fgk_product {
-	const float   *kern;
-	const int32_t *kidx;
-	int32_t        kvw;
-	int32_t        conj;
+	const void *spec; /* float2[L] */
 } fgk_product;
+
+/* spec[m] = bin m of a kernel buffer (re at kern[kidx[m]], im kvw floats
+ * later), conjugated when conj is set: the natural-order copy the product
+ * reads with one coalesced load per bin */
+int fgk_launch_spectrum_natural(const float *kern, const int32_t *kidx, int kvw, uint32_t L, int conj, void *spec,
+                                void *stream);
 
 /* A three-level item: passes A, B, C through two scratch areas; B tiles
  * wait for every A tile of the item, C tiles for every B tile. */

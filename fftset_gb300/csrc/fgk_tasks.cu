@@ -4,6 +4,27 @@
  * (fgk_tasks_{fc,ff,ic,if}[w].cu). */
 #include "fgk_tasks.cuh"
 
+namespace fgk {
+__global__ void spectrum_natural(const float *__restrict__ kern, const int32_t *__restrict__ kidx, int kvw, uint32_t L,
+                                 int conj, float2 *spec)
+{
+	for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < L; m += gridDim.x * blockDim.x) {
+		const int o = __ldg(kidx + m);
+		const float im = __ldg(kern + o + kvw);
+		spec[m] = make_float2(__ldg(kern + o), conj ? -im : im);
+	}
+}
+} /* namespace fgk */
+
+extern "C" int fgk_launch_spectrum_natural(const float *kern, const int32_t *kidx, int kvw, uint32_t L, int conj,
+                                           void *spec, void *stream)
+{
+	const uint32_t grid = (L + 255) / 256 < 1024 ? (L + 255) / 256 : 1024;
+	fgk::spectrum_natural<<<grid, 256, 0, (cudaStream_t)stream>>>(kern, kidx, kvw, L, conj, (float2 *)spec);
+	fgk_count_launch();
+	return (int)cudaGetLastError();
+}
+
 extern "C" int fgk_launch_tasks_fc(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ff(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ic(FGKT_LAUNCH_ARGS);

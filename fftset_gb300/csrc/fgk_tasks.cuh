@@ -305,12 +305,10 @@ __device__ __forceinline__ void tk_signal(int *ctr)
 	}
 }
 
-/* v times bin m of the product's kernel spectrum (or its conjugate) */
+/* v times bin m of the product's natural-order spectrum */
 __device__ __forceinline__ float2 tk_product(const fgk_product &pr, uint32_t m, float2 v)
 {
-	const int o = __ldg(pr.kidx + m);
-	const float2 k = make_float2(__ldg(pr.kern + o), __ldg(pr.kern + o + pr.kvw));
-	return pr.conj ? cmulc(v, k) : cmul(v, k);
+	return cmul(v, __ldg(reinterpret_cast<const float2 *>(pr.spec) + m));
 }
 
 /* ---- SMALL: whole items side by side ---------------------------------- */
@@ -452,7 +450,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		const int k1 = k1base + lane;
 		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * (uint32_t)k2;
 		if (!inverse) {
-			if (prod.kern)
+			if (prod.spec)
 				v = tk_product(prod, m, v);
 			if (!freq)
 				__stcs(o2 + m, v);
@@ -604,7 +602,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 		const int k3 = j + q * nbf;
 		const uint32_t m = (uint32_t)k1 + (uint32_t)L1 * ((uint32_t)k2 + (uint32_t)L2 * k3);
 		if (!inverse) {
-			if (prod.kern)
+			if (prod.spec)
 				v = tk_product(prod, m, v);
 			if (!freq)
 				__stcs(o2 + m, v);
