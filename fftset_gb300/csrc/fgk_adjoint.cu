@@ -43,9 +43,9 @@ __global__ void kg_spec_partial(const float2 *__restrict__ S, const float2 *__re
 /* out = sum over the P partials, in natural order (pack == 0) or in the
  * FREQ_OFFSET_REAL forward layout from packed-sequence bins (pack == 1).
  * A CTA covers KG_BINS bins with KG_SPLIT threads per bin, each summing every
- * KG_SPLIT-th partial (independent loads in flight), then the KG_SPLIT sums
- * of a bin are added in shared memory in a fixed order. */
-constexpr int KG_BINS = 32, KG_SPLIT = 8;
+ * KG_SPLIT-th partial (a warp reads 128-byte runs of two rows), then the
+ * KG_SPLIT sums of a bin are added in shared memory in a fixed order. */
+constexpr int KG_BINS = 16, KG_SPLIT = 32;
 __global__ void __launch_bounds__(KG_BINS *KG_SPLIT) kg_reduce(const float2 *__restrict__ partials, uint32_t P,
                                                               uint32_t L, int pack, float2 *out)
 {

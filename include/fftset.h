@@ -10,7 +10,14 @@
  * are used in place on the fftset's CUDA stream; host buffers are staged
  * through device memory. Calls block until their results are in the output
  * buffer, like the reference's CPU calls, unless fftset_set_blocking(fc, 0)
- * is used (device buffers only; completion is then ordered on the stream). */
+ * is used (device buffers only; completion is then ordered on the stream).
+ *
+ * Threads: the execution calls (forward, inverse, get_kernel, conv, their
+ * batched forms, the ragged execute, the adjoint, overlap-add) may be made
+ * from several threads at once on one fftset, given distinct output buffers,
+ * as the reference promises for its own (README.md:38); all of them are
+ * ordered on the fftset's one stream. Creating plans and batches, changing
+ * settings and the autotuners are not thread-safe, as in the reference. */
 #ifndef FFTSET_H
 #define FFTSET_H
 
