@@ -640,20 +640,33 @@ int fs_is_device_ptr(const void *ptr)
 	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-/* Pinned (page-locked, registered) host memory: kernels reach it directly
- * over the host link; *dev receives the address kernels use. Pageable host
- * memory and device memory return 0. */
-static int fs_pinned_host(const void *ptr, const void **dev)
+/* What a call's buffer is, from one pointer-attribute query: device or
+ * managed memory (used in place), pinned host memory (kernels reach it over
+ * the host link at `kaddr`), or pageable host memory (staged). */
+struct fs_ptrinfo {
+	int         dev;    /* device or managed (NULL counts as device) */
+	int         pinned; /* page-locked host memory with a device address */
+	const void *kaddr;  /* the address kernels use */
+};
+
+static struct fs_ptrinfo fs_classify(const void *ptr)
 {
+	struct fs_ptrinfo pi = {1, 0, ptr};
 	struct cudaPointerAttributes a;
-	if (ptr == NULL || cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+	if (ptr == NULL)
+		return pi;
+	pi.dev = 0;
+	if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
 		cudaGetLastError();
-		return 0;
+		return pi;
 	}
-	if (a.type != cudaMemoryTypeHost || a.devicePointer == NULL)
-		return 0;
-	*dev = a.devicePointer;
-	return 1;
+	if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+		pi.dev = 1;
+	else if (a.type == cudaMemoryTypeHost && a.devicePointer != NULL) {
+		pi.pinned = 1;
+		pi.kaddr = a.devicePointer;
+	}
+	return pi;
 }
 
 int fs_stage_reserve(struct fs_impl *fs, int slot, size_t bytes)
@@ -905,8 +918,10 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 		return FFTSET_OK;
 	in_span = (size_t)(count - 1) * in_stride + nf;
 	out_span = (size_t)(count - 1) * out_stride + nf;
+	/* one query per buffer, whatever path the call takes */
+	const struct fs_ptrinfo pin = fs_classify(in), pout = fs_classify(out), pkern = fs_classify(kern);
 
-	if (fs_is_device_ptr(in) && fs_is_device_ptr(out) && (kern == NULL || fs_is_device_ptr(kern))) {
+	if (pin.dev && pout.dev && pkern.dev) {
 		rc = fs_launch(f, op, out, in, kern, count, in_stride, out_stride);
 		if (rc < 0)
 			return fs_latch(fs, -rc, 0);
@@ -922,21 +937,15 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 
 	/* pinned host buffers (and device ones): resident kernels read and write
 	 * them in place over the host link, no staging copies */
-	if (!f->fourstep) {
-		const void *vin = in, *vout = out, *vkern = kern;
-		const int hin = fs_pinned_host(in, &vin), hout = fs_pinned_host(out, &vout);
-		const int hk = kern != NULL && fs_pinned_host(kern, &vkern);
-		if ((hin || fs_is_device_ptr(in)) && (hout || fs_is_device_ptr(out)) &&
-		    (kern == NULL || hk || fs_is_device_ptr(kern))) {
-			const int v = fs_pick_variant(f, op, count);
-			rc = fs_launch_variant_ex(f, v, op, (float *)vout, (const float *)vin, (const float *)vkern, count,
-			                          in_stride, out_stride, fs->stream, 1);
-			if (rc)
-				return rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
-			if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) != 0)
-				return rc;
-			return fs_check_flag(fs);
-		}
+	if (!f->fourstep && (pin.pinned || pin.dev) && (pout.pinned || pout.dev) && (pkern.pinned || pkern.dev)) {
+		rc = fs_launch_variant_ex(f, fs_pick_variant(f, op, count), op, (float *)pout.kaddr,
+		                          (const float *)pin.kaddr, (const float *)pkern.kaddr, count, in_stride, out_stride,
+		                          fs->stream, 1);
+		if (rc)
+			return rc < 0 ? fs_latch(fs, -rc, 0) : fs_latch(fs, FFTSET_E_CUDA, rc);
+		if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) != 0)
+			return rc;
+		return fs_check_flag(fs);
 	}
 
 	/* pageable host buffers: stage through device memory */
@@ -944,7 +953,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 	staged = 1;
 	if (!f->fourstep && count > 1 && count * nf * sizeof(float) >= 2 * FS_CHUNK_BYTES &&
 	    in_stride >= nf && out_stride >= nf) {
-		if (kern != NULL && !fs_is_device_ptr(kern)) {
+		if (!pkern.dev) {
 			if ((rc = fs_stage_reserve(fs, 2, nf * sizeof(float))))
 				goto done;
 			dkern = (const float *)fs->stage[2];
@@ -954,11 +963,10 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 				goto done;
 			}
 		}
-		rc = fs_exec_pipelined(f, op, out, out_stride, in, in_stride, dkern, count, fs_is_device_ptr(in),
-		                       fs_is_device_ptr(out));
+		rc = fs_exec_pipelined(f, op, out, out_stride, in, in_stride, dkern, count, pin.dev, pout.dev);
 		goto done;
 	}
-	if (!fs_is_device_ptr(in)) {
+	if (!pin.dev) {
 		if ((rc = fs_stage_reserve(fs, 0, in_span * sizeof(float))))
 			goto done;
 		din = (const float *)fs->stage[0];
@@ -969,7 +977,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 			goto done;
 		}
 	}
-	if (kern != NULL && !fs_is_device_ptr(kern)) {
+	if (!pkern.dev) {
 		if ((rc = fs_stage_reserve(fs, 2, nf * sizeof(float))))
 			goto done;
 		dkern = (const float *)fs->stage[2];
@@ -979,7 +987,7 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 			goto done;
 		}
 	}
-	if (!fs_is_device_ptr(out)) {
+	if (!pout.dev) {
 		if ((rc = fs_stage_reserve(fs, 1, out_span * sizeof(float))))
 			goto done;
 		dout = (float *)fs->stage[1];
