@@ -761,14 +761,17 @@ def profile_kernels(torch, fs):
     run("task_kernel forward FREQ 65536 x512 (two-level)", lambda: h.forward_batch(y, x), 2 * B * nf * 4, 1)
     run("task_kernel inverse FREQ 65536 x512 (two-level)", lambda: h.inverse_batch(y, x), 2 * B * nf * 4, 1)
     del x, y
-    # overlap-add: split, conv, merge over 32 M samples with 1025 taps
+    # overlap-add over 32 M samples with 1025 taps: fused, and (blocks of
+    # 1000 samples: K - 1 > B) split, conv, gather
     o = S.create_fft(fs.FREQ_OFFSET_REAL, 1536)
     n, taps = 32 << 20, 1025
     sig, res = buf(n), torch.empty(n + taps - 1, device="cuda")
     K = torch.empty(3072, device="cuda")
     o.conv_get_kernel(K, torch.cat([buf(taps), torch.zeros(3072 - taps, device="cuda")]))
-    run("overlap-add FREQ 1536, 32 M samples, 1025 taps", lambda: o.conv_overlap_add(res, sig, K, taps),
-        8 * n, 3)
+    run("overlap-add FREQ 1536, 32 M samples, 1025 taps (fused: blocks from the signal, results added in)",
+        lambda: o.conv_overlap_add(res, sig, K, taps), 8 * n, 1)
+    run("overlap-add FREQ 1536, 32 M samples, 1025 taps, 1000-sample blocks (split, conv, gather)",
+        lambda: o.conv_overlap_add(res, sig, K, taps, 1000), 8 * n, 3)
     del sig, res
     # ragged batch (first 2000 items of the ragged draw) and the
     # 15,728,640-bin transform (three-level)

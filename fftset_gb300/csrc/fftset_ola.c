@@ -1,8 +1,11 @@
 /* Overlap-add block convolution on top of the batched convolution: the
  * streaming caller the reference is built for (README.md:3; block and
  * transform lengths from fftset_recommend_conv_length, src/fftset.c:145-167).
- * The reference leaves this loop to its users; here it is one call: split
- * into zero-padded blocks (fgk_ola.cu), one fused conv launch for all blocks,
+ * The reference leaves this loop to its users; here it is one call. Where
+ * the size has the compiled fused kernel (static_kernel_ola) and the block
+ * results overlap at most pairwise (K - 1 <= B), one launch reads the blocks
+ * straight from the signal and adds their results into the zeroed output;
+ * otherwise split into zero-padded blocks (fgk_ola.cu), one batched conv,
  * overlap-add gather into the output. */
 #include <stdint.h>
 
@@ -48,6 +51,28 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
 
 	FS_RANGE_PUSH("fftset_fft_conv_overlap_add");
 	pthread_mutex_lock(&fs->lock); /* staging slots 0 and 1 */
+	if (!cplx && B + kernel_length - 1 <= 2 * B &&
+	    (input_buf + samples <= output_buf || output_buf + samples + kernel_length - 1 <= input_buf)) {
+		/* the compiled fused form where the size has it: the blocks are read
+		 * from the signal and their results added into the output, with at
+		 * most two additions per output sample (the output is zeroed first,
+		 * so it must not overlap the signal) */
+		const int v = fgk_static_ola_variant(FGK_MOD_FREQOFF, fft->lfft);
+		if (v >= 0 && v < fft->nvar) {
+			if ((rc = fs_cuda(fs, cudaMemsetAsync(output_buf, 0, (samples + kernel_length - 1) * sizeof(float),
+			                                      fs->stream))) != 0)
+				goto done;
+			rc = fgk_launch_static_ola(&fft->vp[v], v, input_buf, samples, (uint32_t)B,
+			                           (uint32_t)(B + kernel_length - 1), (uint32_t)nblocks,
+			                           samples + kernel_length - 1, kernel_buf, output_buf, fs->stream, fs->num_sms);
+			if (rc == 0)
+				goto finish;
+			if (rc > 0) {
+				rc = fs_latch(fs, FFTSET_E_CUDA, rc);
+				goto done;
+			}
+		}
+	}
 	if ((rc = fs_stage_reserve(fs, 0, bytes)) != 0 || (rc = fs_stage_reserve(fs, 1, bytes)) != 0)
 		goto done;
 	blocks = (float *)fs->stage[0];
@@ -68,6 +93,8 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
 		rc = fs_latch(fs, FFTSET_E_CUDA, rc);
 		goto done;
 	}
+finish:
+	rc = FFTSET_OK;
 	if (fs->blocking) {
 		if ((rc = fs_cuda(fs, cudaStreamSynchronize(fs->stream))) == 0)
 			rc = fs_check_flag(fs);

@@ -245,6 +245,16 @@ int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, size_t g_str
                           size_t x_stride, float *dx, size_t dx_stride, const float *kern, uint32_t count,
                           float *partials, uint32_t max_rows, uint32_t *rows, void *stream, int num_sms);
 
+/* The fused overlap-add (static_kernel_ola): the first compiled variant of
+ * (modulation, L) that has it, or -1; the launch convolves the nblocks
+ * zero-padded blocks of B samples of `in` and adds the first span samples
+ * of each result into `out` (zeroed by the caller) at b B. The caller
+ * launches it only when span <= 2 B (at most two additions per sample, so
+ * the result does not depend on their order). */
+int fgk_static_ola_variant(uint32_t modulation, uint32_t L);
+int fgk_launch_static_ola(const fgk_plan *p, int v, const float *in, uint64_t n, uint32_t B, uint32_t span,
+                          uint32_t nblocks, uint64_t nout, const float *kern, float *out, void *stream, int num_sms);
+
 #ifdef __cplusplus
 }
 #endif

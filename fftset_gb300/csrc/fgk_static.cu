@@ -199,3 +199,39 @@ extern "C" int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, s
 	*rows = (uint32_t)grid;
 	return (int)cudaGetLastError();
 }
+
+extern "C" int fgk_static_ola_variant(uint32_t mod, uint32_t L)
+{
+	const fgk::StaticEntry *e;
+	const int nv = fgk::variants(mod, L, &e);
+	for (int v = 0; v < nv; v++)
+		if (e[v].ola)
+			return v;
+	return -1;
+}
+
+extern "C" int fgk_launch_static_ola(const fgk_plan *p, int v, const float *in, uint64_t n, uint32_t B, uint32_t span,
+                                     uint32_t nblocks, uint64_t nout, const float *kern, float *out, void *stream,
+                                     int num_sms)
+{
+	using namespace fgk;
+	const StaticEntry *e;
+	const int nv = variants(p->modulation, p->L, &e);
+	if (v < 0 || v >= nv || !e[v].ola)
+		return -1;
+	e += v;
+	int per_sm = 0;
+	cudaError_t err = launch_setup((const void *)e->ola, (int)(e->T * e->G), e->ola_smem, &per_sm);
+	if (err != cudaSuccess)
+		return (int)err;
+	if (per_sm < 1)
+		return (int)cudaErrorInvalidConfiguration;
+	uint64_t grid = (uint64_t)per_sm * (uint64_t)num_sms;
+	const uint64_t need = ((uint64_t)nblocks + e->G - 1) / e->G;
+	if (grid > need)
+		grid = need;
+	OlaArgs a{in, n, B, span, nblocks, nout, kern, out};
+	e->ola<<<(unsigned)grid, e->T * e->G, e->ola_smem, (cudaStream_t)stream>>>(*p, a);
+	fgk_count_launch();
+	return (int)cudaGetLastError();
+}

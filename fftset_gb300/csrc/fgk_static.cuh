@@ -590,9 +590,8 @@ __device__ __forceinline__ void pp_stage(int tid, const float2 *tws, Ld &&ld, St
  * j + p L/R and the last stage's butterfly j writes the points j + q L/R
  * (its ns is L/R), so every factor is mods[j] e^{-j pi p / (2R)}: one table
  * read per butterfly and compile-time constants. */
-template <class C, int OP, class St>
-__device__ __forceinline__ void pp_first_modc(int tid, const FirstLoad<C, OP, false> &first, const float2 *mods,
-                                              St &&st)
+template <class C, int OP, class First, class St>
+__device__ __forceinline__ void pp_first_modc(int tid, const First &first, const float2 *mods, St &&st)
 {
 	constexpr int L = C::L, R = C::fr(0), NBF = L / R;
 	constexpr int NB = (NBF + C::T - 1) / C::T;
@@ -758,6 +757,125 @@ __device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float
 			}
 		}
 		gsync<C>(g);
+	}
+}
+
+/* ---- overlap-add, fused into the convolution ---------------------------
+ * Block b of a real signal (FREQ_OFFSET_REAL): its first stage reads the
+ * signal at b B directly, zero past B samples (or past the signal's end), so
+ * the zero-padded blocks are never written out; its last stage adds the
+ * first span = B + K - 1 samples of the block's result into the output at
+ * b B with atomicAdd. The host launches this only when span <= 2 B: every
+ * output sample then receives at most two additions into a zeroed output,
+ * and floating-point addition of two terms does not depend on their order,
+ * so the result is deterministic and equals the unfused split / convolution
+ * / gather bit for bit. The compiled ping-pong configurations with constant
+ * modulation (MODC) provide the stages. */
+struct OlaArgs {
+	const float *in;      /* the signal, n samples */
+	uint64_t     n;
+	uint32_t     B, span; /* block length; result samples added per block */
+	uint32_t     nblocks;
+	uint64_t     nout;    /* n + K - 1 */
+	const float *kern;
+	float       *out;     /* zero when the launch starts */
+};
+
+/* the zero-padded block as the first stage reads it */
+struct OlaLoad {
+	const float *x;
+	uint32_t     valid; /* samples of the signal in this block */
+	__device__ __forceinline__ float ld(int i) const { return (uint32_t)i < valid ? __ldcs(x + i) : 0.f; }
+};
+
+template <class C>
+__global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_ola(const fgk_plan p, OlaArgs a)
+{
+	static_assert(C::PP && C::MODC && C::MOD == FGK_MOD_FREQOFF, "the fused overlap-add uses the MODC ping-pong forms");
+	extern __shared__ float2 smem[];
+	using Lay = Layout<C, FGK_OP_CONV>;
+	constexpr int L = C::L, N = C::N;
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *exb = ks + Lay::KS;
+	StaticArgs sa{};
+	sa.kern = a.kern;
+	stage_tables<C, FGK_OP_CONV>(p, sa, smem, mods, ks);
+	__syncthreads();
+
+	const int g = threadIdx.x / C::T;
+	const int tid = C::wt((int)threadIdx.x - g * C::T, g);
+	float2 *buf0 = exb + (size_t)(2 * g) * C::SLOTS;
+	float2 *buf1 = buf0 + C::SLOTS;
+	for (uint64_t t = (uint64_t)blockIdx.x * C::G + g; t < a.nblocks; t += (uint64_t)gridDim.x * C::G) {
+		const uint64_t base = t * a.B;
+		const OlaLoad first{a.in + base, base + a.B <= a.n ? a.B : (uint32_t)(a.n - base)};
+		const uint32_t lim = base + a.span <= a.nout ? a.span : (uint32_t)(a.nout - base);
+		float *y = a.out + base;
+		const Ex<C> b0{buf0};
+		pp_first_modc<C, FGK_OP_CONV>(tid, first, mods, [&](int i, float2 v) { b0.put(i, v); });
+		gsync<C>(g);
+		pp_fwd<C, 1, N - 1>(tid, g, buf0, buf1, tws);
+		const Ex<C> src{((N - 2) & 1) ? buf1 : buf0}, dst{((N - 2) & 1) ? buf0 : buf1};
+		{
+			constexpr int R = C::fr(N - 1), NS = C::fns(N - 1), NBF = L / R;
+			constexpr int NB = (NBF + C::T - 1) / C::T;
+			constexpr bool FULL = (NBF % C::T) == 0;
+#pragma unroll 2
+			for (int b = 0; b < NB; b++) {
+				const int j = tid + b * C::T;
+				if (FULL || j < NBF) {
+					float2 v[R];
+#pragma unroll
+					for (int q = 0; q < R; q++)
+						v[q] = src(j + q * NBF);
+					if constexpr (NS > 1)
+						twiddle_in<C, R, NS>(v, tws + C::ftw_off(N - 1), j);
+					Radix<R>::run(v);
+#pragma unroll
+					for (int q = 0; q < R; q++)
+						v[q] = conjf2(cmul(v[q], ks[j + q * NBF]));
+					Radix<R>::run(v);
+#pragma unroll
+					for (int q = 0; q < R; q++)
+						dst.put(j * R + q, v[q]);
+				}
+			}
+			gsync<C>(g);
+		}
+		pp_inv<C, 1, N - 1>(tid, g, buf0, buf1, tws);
+		{
+			constexpr int RL = C::ir(N - 1), NSL = C::ins(N - 1), NBFL = L / RL;
+			static_assert(NSL == NBFL, "the last stage's ns is L/R");
+			constexpr int RD = (2 * N - 3) & 1;
+			constexpr int NB = (NBFL + C::T - 1) / C::T;
+			constexpr bool FULL = (NBFL % C::T) == 0;
+			const Ex<C> last{RD ? buf1 : buf0};
+#pragma unroll 2
+			for (int b = 0; b < NB; b++) {
+				const int j = tid + b * C::T;
+				if (FULL || j < NBFL) {
+					float2 v[RL];
+#pragma unroll
+					for (int q = 0; q < RL; q++)
+						v[q] = last(j + q * NBFL);
+					twiddle_in<C, RL, NSL>(v, tws + C::itw_off(N - 1), j);
+					Radix<RL>::run(v);
+					mod_steps<RL>(v, mods[j]);
+#pragma unroll
+					for (int q = 0; q < RL; q++) {
+						const uint32_t i0 = (uint32_t)(j + q * NBFL), i1 = i0 + (uint32_t)L;
+						if (i0 < lim)
+							atomicAdd(y + i0, v[q].x);
+						if (i1 < lim)
+							atomicAdd(y + i1, v[q].y);
+					}
+				}
+			}
+			if constexpr (RD == 0)
+				gsync<C>(g);
+		}
 	}
 }
 
@@ -1073,6 +1191,7 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_adj(const fgk_pla
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
 typedef void (*kgrad_fn)(const fgk_plan, KgradArgs);
 typedef void (*adj_fn)(const fgk_plan, AdjArgs);
+typedef void (*ola_fn)(const fgk_plan, OlaArgs);
 
 struct StaticEntry {
 	uint32_t  mod, L, T, G, n, tma;
@@ -1083,6 +1202,8 @@ struct StaticEntry {
 	size_t    kgrad_smem;
 	adj_fn    adj; /* the one-pass adjoint (input and taps gradients), or null */
 	size_t    adj_smem;
+	ola_fn    ola; /* the fused overlap-add, or null */
+	size_t    ola_smem;
 };
 
 template <class C, int OP> constexpr size_t smem_bytes()
@@ -1149,6 +1270,16 @@ template <class C> StaticEntry with_kgrad(StaticEntry e)
 	e.kgrad_smem = kgrad_smem_bytes<C>();
 	e.adj = static_kernel_adj<C>;
 	e.adj_smem = AdjLayout<C>::BYTES;
+	return e;
+}
+
+/* adds the fused overlap-add kernel to an entry (MODC ping-pong
+ * FREQ_OFFSET_REAL configurations) */
+template <class C> StaticEntry with_ola(StaticEntry e)
+{
+	static_assert(smem_bytes<C, FGK_OP_CONV>() <= FGK_SMEM_LIMIT, "overlap-add kernel exceeds shared memory");
+	e.ola = static_kernel_ola<C>;
+	e.ola_smem = smem_bytes<C, FGK_OP_CONV>();
 	return e;
 }
 

@@ -525,12 +525,16 @@ def test_pinned_host_buffers_in_place_access(gpu_set, mod, L, op):
     assert np.array_equal(y.numpy()[:, 2 * L:], x.numpy()[:, 2 * L:])
 
 
-@pytest.mark.parametrize("mod,L,K,blk", [(1, 1536, 401, 0), (1, 1536, 2048, 0), (1, 4096, 900, 1000),
-                                         (0, 1024, 200, 0), (1, 768, 1, 0)])
+@pytest.mark.parametrize("mod,L,K,blk", [(1, 1536, 401, 0), (1, 1536, 1025, 0), (1, 1536, 1025, 1500),
+                                         (1, 1536, 2048, 0), (1, 4096, 900, 1000), (0, 1024, 200, 0),
+                                         (1, 768, 1, 0)])
 def test_overlap_add_linear_convolution(gpu_set, mod, L, K, blk):
     """fftset_fft_conv_overlap_add: complex_bins times the linear convolution
     of a long signal (several hundred blocks, ragged last block) with a K-tap
-    kernel, against FP64 np.convolve."""
+    kernel, against FP64 np.convolve. FREQ_OFFSET_REAL at 1536 bins with
+    K - 1 <= B runs the fused kernel (blocks read from the signal, results
+    added into the output); K = 2048 at 1536 bins (K - 1 > B) and the other
+    sizes run split, batched convolution and gather."""
     import torch
     f = gpu_set.create_fft(mod, L)
     N = L if mod == 0 else 2 * L
