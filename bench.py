@@ -449,6 +449,39 @@ def workload_conv_large(fs, torch, peak):
             "relL2_vs_fp64_4blocks": rel, "tolerance": O.tolerance(N)}
 
 
+def workload_overlap_add(fs, torch, peak):
+    """Overlap-add block convolution of a 32 M-sample real signal with a
+    1025-tap decaying Gaussian kernel through a 1536-bin FREQ_OFFSET_REAL
+    plan (blocks of 2048 samples): the fused kernel. Bytes: one read of the
+    signal and one write of the result."""
+    from oracle import oracle as O
+    L, n, taps = 1536, 32 << 20, 1025
+    rng = np.random.default_rng(13)
+    x_np = rng.standard_normal(n).astype(np.float32)
+    h_np = np.zeros(2 * L, np.float32)
+    h_np[:taps] = rng.standard_normal(taps) * np.exp(-np.arange(taps) / 200.0)
+    x, h = torch.from_numpy(x_np).cuda(), torch.from_numpy(h_np).cuda()
+    S = fs.FftSet()
+    S.set_stream(torch.cuda.current_stream())
+    f = S.create_fft(fs.FREQ_OFFSET_REAL, L)
+    K = torch.empty_like(h)
+    f.conv_get_kernel(K, h)
+    y = torch.empty(n + taps - 1, device="cuda")
+    S.set_blocking(False)
+    f.conv_overlap_add(y, x, K, taps)
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, lambda: f.conv_overlap_add(y, x, K, taps), 10, torch.cuda.current_stream())
+    S.check()
+    m = 1 << 16  # the first samples against FP64 np.convolve
+    want = L * np.convolve(x_np[:m].astype(np.float64), h_np[:taps].astype(np.float64))[:m]
+    rel = O.rel_l2(y[:m].cpu().numpy(), want)
+    S.close()
+    nbytes = 4 * n + 4 * (n + taps - 1)
+    return {"workload": "freqoffsetreal_overlap_add_L1536_32M_samples_1025_taps", "ms": ms,
+            "gbs": nbytes / ms / 1e6, "frac_of_peak": nbytes / ms / 1e6 / peak,
+            "relL2_vs_fp64_first_65536": rel, "tolerance": O.tolerance(2 * L)}
+
+
 def dist_setup(n_gpus):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -597,7 +630,7 @@ def run_gb300(args):
             del x, y, xh, yh
             torch.cuda.empty_cache()
             for fn in (workload_percall_complex1024, workload_ragged, workload_large, workload_adjoint,
-                       workload_conv_large):
+                       workload_conv_large, workload_overlap_add):
                 try:
                     r = fn(fs, torch, peak)
                     others[r.pop("workload")] = r

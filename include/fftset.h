@@ -221,8 +221,12 @@ int fftset_fft_conv_adjoint_batch(const struct fftset_fft *fft, float *grad_inpu
  * N - kernel_length + 1, the most that does not wrap), each zero-padded to N;
  * one batched convolution; the results are overlap-added into output_buf,
  * samples + kernel_length - 1 samples, complex_bins times the linear
- * convolution (the scale of fftset_fft_conv). Device buffers; uses 2 x
- * blocks x N samples of the fftset's staging memory. */
+ * convolution (the scale of fftset_fft_conv). Device buffers. Where the
+ * plan has a compiled fused kernel (FREQ_OFFSET_REAL, 1536 bins) and
+ * kernel_length - 1 <= block_length, one launch reads the blocks from the
+ * signal and adds their results into output_buf (used when output_buf does
+ * not overlap input_buf); otherwise the blocks go through 2 x blocks x N
+ * samples of the fftset's staging memory. */
 int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf, const float *input_buf,
                                 size_t samples, const float *kernel_buf, unsigned kernel_length,
                                 unsigned block_length);
