@@ -82,6 +82,11 @@ template <int MOD_, int L_, int T_, int G_, int TWG_, int MODE_, int... Rs> stru
 	static __host__ __device__ constexpr int itw_off(int s) { return PAL ? ftw_off(s) : itw_off_full(s); }
 	static constexpr int TW_TOTAL = PAL ? ftw_off(N) : itw_off_full(N);
 	static constexpr int SLOTS = L + L / 16 + 1; /* padded exchange buffer */
+	/* modulation factors staged in shared memory: all L, or with constant
+	 * modulation only those of the first and last stages' butterflies
+	 * (mods[j], j < L / R for R the first and last radices) */
+	static constexpr int NMODS =
+	    MOD == FGK_MOD_FREQOFF ? (MODC ? L / (R[0] < R[N - 1] ? R[0] : R[N - 1]) : L) : 0;
 	static __host__ __device__ constexpr int slot(int i) { return i + (i >> 4); }
 };
 
@@ -429,7 +434,7 @@ __device__ __forceinline__ void stage_tables(const fgk_plan &p, const StaticArgs
 		stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
 	if constexpr (C::MOD == FGK_MOD_FREQOFF) {
 		const float2 *gm = (const float2 *)p.modtw;
-		for (int i = threadIdx.x; i < L; i += blockDim.x)
+		for (int i = threadIdx.x; i < C::NMODS; i += blockDim.x)
 			mods[i] = __ldg(gm + i);
 	}
 	if constexpr (OP == FGK_OP_CONV || OP == FGK_OP_CORR) {
@@ -449,7 +454,7 @@ template <class C, int OP> struct Layout {
 	static constexpr bool FREQ = C::MOD == FGK_MOD_FREQOFF;
 	static constexpr bool CONV = OP == FGK_OP_CONV || OP == FGK_OP_CORR;
 	static constexpr size_t TW = C::TWG ? 0 : (size_t)C::TW_TOTAL; /* float2 */
-	static constexpr size_t MODS = FREQ ? C::L : 0;
+	static constexpr size_t MODS = (size_t)C::NMODS;
 	static constexpr size_t KS = CONV ? C::L : 0;
 	static constexpr size_t TABLES = TW + MODS + KS;
 	/* TMA mode: per group two buffers, each holding a raw input block (2L

@@ -13,7 +13,7 @@
  * 4096 bins a thread runs one radix-16 butterfly per stage with all 256
  * threads busy, and the extra multiplies lengthen it. The chain is a
  * palindrome, so its twiddles are staged once. V0 also carries the
- * taps-gradient kernel of the adjoint (static_kernel_kgrad). */
+ * adjoint's one-pass kernels (static_kernel_adj, static_kernel_kgrad). */
 #include "fgk_static.cuh"
 
 namespace fgk {
@@ -24,22 +24,33 @@ using V3 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 3, 0, 0, 16, 16, 16>;
 using V4 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 6, 2, 16, 16, 16>;
 using V5 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 1, 0, 2, 16, 16, 16>;
 using V6 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 1, 1, 16, 16, 16>;
+/* ping-pong with both table forms and two groups (the constant modulation
+ * stages 256 factors, not 4096, which leaves room for the second group):
+ * the fastest inverse (2048 / 8192 blocks: 0.0358 / 0.106 ms against V0's
+ * 0.0404 / 0.121), listed first for that op only; for conv and forward it
+ * measured slower than V0 (0.061 / 0.195 and 0.050 / 0.146 ms). V8: the
+ * same with the modulation form only (inverse 0.0364 / 0.109). */
+using V7 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 6, 2, 16, 16, 16>;
+using V8 = SCfg<FGK_MOD_FREQOFF, 4096, 256, 2, 4, 2, 16, 16, 16>;
 
 int static_entries_4096(const StaticEntry **out)
 {
-	static StaticEntry t[7];
+	static StaticEntry t[10];
 	static bool init = false;
 	if (!init) {
-		t[0] = with_kgrad<V0>(make_entry<V0, OPS_ALL>());
-		t[1] = make_entry<V1, OPS_ALL>();
-		t[2] = make_entry<V2, OPS_CONV_CORR>();
-		t[3] = make_entry<V3, OPS_CONV_CORR>();
-		t[4] = make_entry<V4, OPS_ALL>();
-		t[5] = make_entry<V5, OPS_CONV_CORR>();
-		t[6] = make_entry<V6, OPS_ALL>();
+		t[0] = make_entry<V7, 1 << FGK_OP_INVERSE>();
+		t[1] = with_kgrad<V0>(make_entry<V0, OPS_ALL>());
+		t[2] = make_entry<V1, OPS_ALL>();
+		t[3] = make_entry<V2, OPS_CONV_CORR>();
+		t[4] = make_entry<V3, OPS_CONV_CORR>();
+		t[5] = make_entry<V4, OPS_ALL>();
+		t[6] = make_entry<V5, OPS_CONV_CORR>();
+		t[7] = make_entry<V6, OPS_ALL>();
+		t[8] = make_entry<V7, OPS_ALL>();
+		t[9] = make_entry<V8, OPS_ALL>();
 		init = true;
 	}
 	*out = t;
-	return 7;
+	return 10;
 }
 } /* namespace fgk */
