@@ -129,6 +129,7 @@ int fftset_init(struct fftset *fc)
 	}
 	fs->stream = fs->own_stream;
 	fs->spin_limit = 1u << 22; /* about a second */
+	fs->task_shape = -1;
 	fs->blocking = 1;
 	fs->layout_vw = 4;
 	fs->device = dev;
@@ -1182,6 +1183,15 @@ int fftset__test_set_spin_limit(struct fftset *fc, unsigned polls)
 	if (!fs || polls == 0)
 		return FFTSET_E_INVALID;
 	fs->spin_limit = polls;
+	return FFTSET_OK;
+}
+
+int fftset__test_set_task_shape(struct fftset *fc, int shape)
+{
+	struct fs_impl *fs = fs_of(fc);
+	if (!fs || shape < -1 || shape > 1)
+		return FFTSET_E_INVALID;
+	fs->task_shape = shape;
 	return FFTSET_OK;
 }
 

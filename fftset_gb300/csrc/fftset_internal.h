@@ -91,6 +91,7 @@ struct fs_impl {
 	pthread_mutex_t    lock;
 	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
 	uint32_t           spin_limit; /* polls of a task kernel's bounded waits (fgk_launch_tasks) */
+	int                task_shape; /* ragged task CTAs: -1 by the list, 0 narrow, 1 wide */
 	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
@@ -152,6 +153,9 @@ void fftset__test_live_allocations(long *host, long *device);
  * (launches made afterwards), and a ragged batch without its tasks of one
  * kind (the tasks that wait on them then time out). */
 int  fftset__test_set_spin_limit(struct fftset *fc, unsigned polls);
+/* CTA shape of the task lists of later ragged creates: -1 chosen by the
+ * list (wide when it holds three-level items), 0 narrow, 1 wide */
+int  fftset__test_set_task_shape(struct fftset *fc, int shape);
 int  fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind);
 #if !defined(FS_ALLOC_IMPL) && !defined(__cplusplus)
 #include <stdlib.h>

@@ -182,6 +182,8 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		if (bins[i] > 65536)
 			rb->wide = 1; /* three-level items measured faster on wide CTAs */
 	}
+	if (fs->task_shape >= 0)
+		rb->wide = fs->task_shape;
 	qsort(order, n, sizeof(*order), fsr_cmp);
 
 	/* plans, items and big items; SMALL tasks are counted here, listed below */

@@ -78,6 +78,42 @@ def test_ragged_equals_single_calls(fftset_lib, gpu_set):
     rb.close()
 
 
+@pytest.mark.parametrize("mod", [0, 1])
+def test_ragged_both_task_shapes(fftset_lib, mod):
+    """The list's CTA shape forced either way (narrow 128-thread or wide
+    256-thread task CTAs), two-level and three-level items alike: every item
+    against FP64, in both directions."""
+    import ctypes as C
+    import torch
+    L_ = fftset_lib.library()
+    L_.fftset__test_set_task_shape.restype = C.c_int
+    L_.fftset__test_set_task_shape.argtypes = [fftset_lib._P, C.c_int]
+    sizes = [int(s) for s in draw_sizes(60, seed=11 + mod)]
+    sizes[:3] = [262144, 65536, 19683]
+    offs, total = layout(sizes)
+    x = np.random.default_rng(12).uniform(-1, 1, total).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    S = fftset_lib.FftSet()
+    try:
+        for shape in (0, 1):
+            assert L_.fftset__test_set_task_shape(S.handle, shape) == 0
+            for op in (fftset_lib.OP_FORWARD, fftset_lib.OP_INVERSE):
+                rb = fftset_lib.Ragged(S, mod, op, sizes, offs, offs)
+                y = torch.full_like(xd, 3.0)
+                rb.execute(y, xd)
+                torch.cuda.synchronize()
+                yh = y.cpu().numpy()
+                for L, o in zip(sizes, offs):
+                    xi = x[o:o + 2 * L]
+                    want = O.forward64(mod, xi) if op == fftset_lib.OP_FORWARD else O.inverse64(mod, xi)
+                    assert O.rel_l2(yh[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (shape, L, op)
+                rb.close()
+        assert L_.fftset__test_set_task_shape(S.handle, 2) != 0
+        S.check()
+    finally:
+        S.close()
+
+
 def test_ragged_rejects_bad_input(fftset_lib, gpu_set):
     with pytest.raises(fftset_lib.FftsetError):
         fftset_lib.Ragged(gpu_set, 0, fftset_lib.OP_FORWARD, [64, 7], [0, 200], [0, 200])
