@@ -329,7 +329,7 @@ int fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f)
 	fgk_plan3 *p = &f->p3;
 	const unsigned L = f->lfft;
 	const uint32_t modulation = f->modulator->freq_offset_real ? FGK_MOD_FREQOFF : FGK_MOD_COMPLEX;
-	enum { NT = 15 };
+	enum { NT = 8 };
 	size_t cnt[NT], off[NT + 1], total, i, k, all = 0;
 	float *h = NULL, *w[NT];
 	char *d = NULL;
@@ -343,25 +343,12 @@ int fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f)
 	if (fgk_plan_threestep(p, L, modulation))
 		return FFTSET_E_UNSUPPORTED;
 	L12 = p->L1 * p->L2;
-	p->tshift = 1;
-	while (((uint64_t)1 << (2 * p->tshift)) < L)
-		p->tshift++;
-	p->ushift = 1;
-	while (((uint64_t)1 << (2 * p->ushift)) < L12)
-		p->ushift++;
-	/* tw1 tw2 tw3 thi tlo uhi ulo tq1 tq2 ma mb mc oa ob oc */
-	cnt[0] = fgk_chain_twiddles(&p->c1, NULL);
-	cnt[1] = fgk_chain_twiddles(&p->c2, NULL);
-	cnt[2] = fgk_chain_twiddles(&p->c3, NULL);
-	cnt[3] = (L + (1u << p->tshift) - 1) >> p->tshift;
-	cnt[4] = (size_t)1 << p->tshift;
-	cnt[5] = (L12 + (1u << p->ushift) - 1) >> p->ushift;
-	cnt[6] = (size_t)1 << p->ushift;
-	cnt[7] = p->nq1;
-	cnt[8] = p->nq2;
-	cnt[9] = cnt[12] = p->L1;
-	cnt[10] = cnt[13] = p->L2;
-	cnt[11] = cnt[14] = p->L3;
+	/* tq1 tq2 ma mb mc oa ob oc */
+	cnt[0] = p->nq1;
+	cnt[1] = p->nq2;
+	cnt[2] = cnt[5] = p->L1;
+	cnt[3] = cnt[6] = p->L2;
+	cnt[4] = cnt[7] = p->L3;
 	total = fs_align(sizeof(fgk_plan3));
 	for (i = 0; i < NT; i++) {
 		off[i] = total;
@@ -374,44 +361,25 @@ int fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f)
 	w[0] = h;
 	for (i = 1; i < NT; i++)
 		w[i] = w[i - 1] + 2 * (cnt[i - 1] ? cnt[i - 1] : 1);
-	fgk_chain_twiddles(&p->c1, w[0]);
-	fgk_chain_twiddles(&p->c2, w[1]);
-	fgk_chain_twiddles(&p->c3, w[2]);
 	{
 		/* table i, entry k: e^{-j 2 pi num(k) / den} (FP64, rounded once) */
 		const double twopi = 2.0 * M_PI;
-		for (k = 0; k < cnt[3]; k++) {
-			double a = -twopi * (double)(k << p->tshift) / (double)L;
-			w[3][2 * k] = (float)cos(a), w[3][2 * k + 1] = (float)sin(a);
-		}
-		for (k = 0; k < cnt[4]; k++) {
-			double a = -twopi * (double)k / (double)L;
-			w[4][2 * k] = (float)cos(a), w[4][2 * k + 1] = (float)sin(a);
-		}
-		for (k = 0; k < cnt[5]; k++) {
-			double a = -twopi * (double)(k << p->ushift) / (double)L12;
-			w[5][2 * k] = (float)cos(a), w[5][2 * k + 1] = (float)sin(a);
-		}
-		for (k = 0; k < cnt[6]; k++) {
-			double a = -twopi * (double)k / (double)L12;
-			w[6][2 * k] = (float)cos(a), w[6][2 * k + 1] = (float)sin(a);
-		}
-		for (k = 0; k < cnt[7]; k++) {
+		for (k = 0; k < cnt[0]; k++) {
 			double a = -twopi * (double)k / (double)p->nq1;
-			w[7][2 * k] = (float)cos(a), w[7][2 * k + 1] = (float)sin(a);
+			w[0][2 * k] = (float)cos(a), w[0][2 * k + 1] = (float)sin(a);
 		}
-		for (k = 0; k < cnt[8]; k++) {
+		for (k = 0; k < cnt[1]; k++) {
 			double a = -twopi * (double)k / (double)p->nq2;
-			w[8][2 * k] = (float)cos(a), w[8][2 * k + 1] = (float)sin(a);
+			w[1][2 * k] = (float)cos(a), w[1][2 * k + 1] = (float)sin(a);
 		}
 		/* modulation: in e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2 L1 L2)}, e^{-j pi n3/(2L)};
 		 * out e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2 L3)}, e^{-j pi k3/(2 L3)} */
 		{
 			const double den[6] = {2.0 * p->L1, 2.0 * L12, 2.0 * L, 2.0 * L, 2.0 * p->L2 * p->L3, 2.0 * p->L3};
 			for (i = 0; i < 6; i++)
-				for (k = 0; k < cnt[9 + i]; k++) {
+				for (k = 0; k < cnt[2 + i]; k++) {
 					double a = -M_PI * (double)k / den[i];
-					w[9 + i][2 * k] = (float)cos(a), w[9 + i][2 * k + 1] = (float)sin(a);
+					w[2 + i][2 * k] = (float)cos(a), w[2 + i][2 * k + 1] = (float)sin(a);
 				}
 		}
 	}
@@ -420,8 +388,7 @@ int fs_ensure_threestep(struct fs_impl *fs, struct fftset_fft *f)
 		goto out;
 	}
 	{
-		const void **dst[NT] = {&p->tw1, &p->tw2, &p->tw3, &p->thi, &p->tlo, &p->uhi, &p->ulo, &p->tq1, &p->tq2,
-		                        &p->ma,  &p->mb,  &p->mc,  &p->oa,  &p->ob,  &p->oc};
+		const void **dst[NT] = {&p->tq1, &p->tq2, &p->ma, &p->mb, &p->mc, &p->oa, &p->ob, &p->oc};
 		for (i = 0; i < NT; i++) {
 			*dst[i] = d + off[i];
 			if (cnt[i] &&

@@ -88,12 +88,8 @@ typedef struct fgk_plan4 {
  *   pass C: DFT_L3 over n3 into X[k1 + L1 k2 + L1 L2 k3]. */
 typedef struct fgk_plan3 {
 	uint32_t    L1, L2, L3, modulation;
-	uint32_t    tshift;          /* w_L^m = thi[m >> tshift] tlo[m & (2^tshift - 1)] */
-	uint32_t    ushift;          /* w_{L1 L2}^m = uhi[m >> ushift] ulo[m & (2^ushift - 1)] */
 	uint32_t    nq1, nq2;        /* R1 L2 and R2 L3, R1 / R2 the last radices of c1 / c2 */
-	fgk_chain   c1, c2, c3;
-	const void *tw1, *tw2, *tw3; /* chain twiddles */
-	const void *thi, *tlo, *uhi, *ulo;
+	fgk_chain   c1, c2, c3;      /* the passes' chains (their twiddles are computed in the kernel) */
 	const void *tq1, *tq2;       /* w_{R1 L2}^m, w_{R2 L3}^m */
 	const void *ma, *mb, *mc;    /* e^{-j pi n1/(2 L1)}, e^{-j pi n2/(2 L1 L2)}, e^{-j pi n3/(2L)} */
 	const void *oa, *ob, *oc;    /* e^{-j pi k1/(2L)}, e^{-j pi k2/(2 L2 L3)}, e^{-j pi k3/(2 L3)} */

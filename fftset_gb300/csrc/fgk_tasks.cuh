@@ -85,34 +85,53 @@ struct Rows {
 	__device__ __forceinline__ int slot(int i, int lane) const { return i * ((1 << ls) + 1) + lane; }
 };
 
-/* v[p] *= w^{p k} (p = 1..R-1) from the butterfly's row t of the stage's
- * twiddle table (t[p-1] = w^{p k}). Radix 8 and above read the entries of
- * p = 1, 2, 4, 8 only and form the others as products (twiddle_powers,
- * fgk_codelets.cuh): 4 instead of 15 table reads for radix 16, which go
- * through an L1 shared with many sizes' tables. */
-template <int R> __device__ __forceinline__ void tk_twiddle(float2 (&v)[R], const float2 *__restrict__ t)
+/* e^{-j pi x} (x = 2 m / D) by CUDA's sincospif */
+__device__ __forceinline__ float2 tk_expi(float x)
 {
-	if constexpr (R >= 8) {
-		float2 w[R];
-		twiddle_powers<R>(w, [&](int p) { return __ldg(t + p - 1); });
+	float sn, cs;
+	sincospif(x, &sn, &cs);
+	return make_float2(cs, -sn);
+}
+
+/* w_D^m = e^{-2 pi j m / D} for 0 <= m < D, x2 = 2 / D: the angle taken
+ * in (-pi, pi] so that its rounding error stays below pi 2^-23 */
+__device__ __forceinline__ float2 tk_wm(uint32_t m, uint32_t D, float x2)
+{
+	const int mm = m > (D >> 1) ? (int)(m - D) : (int)m;
+	return tk_expi((float)mm * x2);
+}
+
+/* v[p] *= w^{p k} (p = 1..R-1), w = e^{-2 pi j / D}, x2 = 2 / D. The
+ * butterfly's base twiddles are computed, not read: w^{k} and (radix 8
+ * and above) w^{8k} by sincospif, w^{2k} and w^{4k} as squares, the other
+ * powers as products (twiddle_powers, fgk_codelets.cuh). A table read
+ * would go through an L1 shared with many sizes' tables and three tiles'
+ * shared memory, and its latency sat on every stage's critical path. */
+template <int R> __device__ __forceinline__ void tk_twiddle(float2 (&v)[R], int k, float x2)
+{
+	const float2 w1 = tk_expi((float)k * x2);
+	const float2 w2 = cmul(w1, w1);
+	float2 w4 = make_float2(1.f, 0.f), w8 = w4;
+	if constexpr (R > 4)
+		w4 = cmul(w2, w2);
+	if constexpr (R > 8)
+		w8 = tk_expi((float)(8 * k) * x2);
+	float2 w[R];
+	twiddle_powers<R>(w, [&](int p) { return p == 1 ? w1 : p == 2 ? w2 : p == 4 ? w4 : w8; });
 #pragma unroll
-		for (int p = 1; p < R; p++)
-			v[p] = cmul(v[p], w[p]);
-	} else {
-#pragma unroll
-		for (int p = 1; p < R; p++)
-			v[p] = cmul(v[p], __ldg(t + p - 1));
-	}
+	for (int p = 1; p < R; p++)
+		v[p] = cmul(v[p], w[p]);
 }
 
 /* Stockham stage over a lane-interleaved tile: element i of lane l at
  * rslot((i << ls) + l); work item w = (butterfly j, lane) with the lane
  * fastest, so a warp's accesses are consecutive slots. */
 template <int R, class A>
-__device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int Lp, int ls, int ns,
-                                           const float2 *__restrict__ tw, int tid, int T, A ad)
+__device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int Lp, int ls, int ns, int tid, int T,
+                                           A ad)
 {
 	const int nbf = Lp / R;
+	const float x2 = 2.0f / (float)(ns * R);
 	const int items = nbf << ls;
 	const int lm = (1 << ls) - 1;
 	for (int w = tid; w < items; w += T) {
@@ -123,7 +142,7 @@ __device__ __forceinline__ void lane_stage(const float2 *src, float2 *dst, int L
 			v[p] = src[ad.slot(j + p * nbf, lane)];
 		const int k = j % ns;
 		if (ns > 1)
-			tk_twiddle<R>(v, tw + k * (R - 1));
+			tk_twiddle<R>(v, k, x2);
 		Radix<R>::run(v);
 		const int base = (j - k) * R + k;
 #pragma unroll
@@ -180,10 +199,10 @@ __device__ __forceinline__ void lane_first(Ld &&ld, float2 *dst, int Lp, int ls,
  * takes consecutive butterflies j of one lane (consecutive outputs k),
  * otherwise consecutive lanes of one butterfly. */
 template <int R, bool JF, class A, class St>
-__device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, int ls, const float2 *__restrict__ tw,
-                                          int tid, int T, A ad)
+__device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, int ls, int tid, int T, A ad)
 {
 	const int nbf = Lp / R;
+	const float x2 = 2.0f / (float)Lp;
 	const int items = nbf << ls;
 	const int lm = (1 << ls) - 1;
 	const float inv = 1.0f / (float)nbf;
@@ -201,7 +220,7 @@ __device__ __forceinline__ void lane_last(const float2 *src, St &&st, int Lp, in
 		for (int p = 0; p < R; p++)
 			v[p] = src[ad.slot(j + p * nbf, lane)];
 		if (nbf > 1)
-			tk_twiddle<R>(v, tw + j * (R - 1));
+			tk_twiddle<R>(v, j, x2);
 		Radix<R>::run(v);
 #pragma unroll
 		for (int q = 0; q < R; q++)
@@ -231,7 +250,7 @@ __device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, i
  * stage is done (all of its reads have returned). Threads with active ==
  * false only take part in the barriers. */
 template <bool JF, class AD, class Ld, class St, class After>
-__device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw, int Lp, int ls, float2 *A,
+__device__ __forceinline__ void tile_chain(const fgk_chain *ch, int Lp, int ls, float2 *A,
                                            float2 *B, int tid, int T, bool active, Ld &&ld, St &&st,
                                            After &&after_first)
 {
@@ -254,7 +273,7 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	for (int s = 1; s < n - 1; s++) {
 		const fgk_stage sm = ch->st[s];
 		if (active)
-			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tw + sm.tw_off, tid, T, ad)));
+			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tid, T, ad)));
 		__syncthreads();
 		float2 *t = src;
 		src = dst;
@@ -262,7 +281,7 @@ __device__ __forceinline__ void tile_chain(const fgk_chain *ch, const float2 *tw
 	}
 	if (active) {
 		const fgk_stage sl = ch->st[n - 1];
-		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tw + sl.tw_off, tid, T, ad)));
+		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tid, T, ad)));
 	}
 }
 
@@ -362,7 +381,7 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 			__stcs(y2 + k, conjf2(v));
 		}
 	};
-	tile_chain<false, Pad>(&pl->fwd, (const float2 *)pl->tw, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
+	tile_chain<false, Pad>(&pl->fwd, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
 	                       pre);
 }
 
@@ -383,8 +402,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 	const float *x = in_base + bg.in_off;
 	const float2 *x2 = reinterpret_cast<const float2 *>(x);
 	const float2 *m1 = (const float2 *)p->m1, *m2 = (const float2 *)p->m2;
-	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo;
-	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
+	const float xL = 2.0f / (float)L;
 	float2 *S = scratch + bg.scratch_off;
 	auto ld = [&](int n1, int lane) {
 		const int n2 = n2base + lane;
@@ -409,12 +427,12 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 			return;
 		const int k1 = j + q * nbf;
 		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
-		const float2 a = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 a = tk_wm(m, L, xL);
 		const float2 w = q ? cmul(a, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : a;
 		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
 		       cmul(v, w));
 	};
-	tile_chain<true, Rows>(&p->c1, (const float2 *)p->tw1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<true, Rows>(&p->c1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                       (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
@@ -474,7 +492,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		for (uintptr_t a = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)tid * 128; a + 128 <= b1; a += (uintptr_t)T * 128)
 			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
 	};
-	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
+	tile_chain<false, Rows>(&p->c2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
 	                        [&] {
 		                        discard();
 		                        pre();
@@ -497,8 +515,9 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
 	const float *x = in_base + hg.in_off;
 	const float2 *x2 = reinterpret_cast<const float2 *>(x);
 	const float2 *ma = (const float2 *)p->ma, *mb = (const float2 *)p->mb, *mc = (const float2 *)p->mc;
-	const float2 *uhi = (const float2 *)p->uhi, *ulo = (const float2 *)p->ulo, *tq = (const float2 *)p->tq1;
-	const uint32_t ush = p->ushift, umask = (1u << ush) - 1;
+	const float2 *tq = (const float2 *)p->tq1;
+	const uint32_t L12 = (uint32_t)L1 * p->L2;
+	const float x12 = 2.0f / (float)L12;
 	float2 *A = scratch + hg.sa;
 	auto ld = [&](int n1, int lane) {
 		const uint32_t c = (uint32_t)(cbase + lane);
@@ -523,11 +542,11 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
 			return;
 		const int n2 = tk_div((int)c, L3, inv3);
 		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
-		const float2 b = cmul(__ldg(uhi + (m >> ush)), __ldg(ulo + (m & umask)));
+		const float2 b = tk_wm(m, L12, x12);
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : b;
 		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
 	};
-	tile_chain<false, Rows>(&p->c1, (const float2 *)p->tw1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(&p->c1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
@@ -545,8 +564,9 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	const uint32_t L23 = (uint32_t)L2 * L3;
 	const int k1g = (int)(tk.a / hg.nb3);
 	const int k1b = k1g * 4, n3b = (int)(tk.a - (uint32_t)k1g * hg.nb3) * 4;
-	const float2 *thi = (const float2 *)p->thi, *tlo = (const float2 *)p->tlo, *tq = (const float2 *)p->tq2;
-	const uint32_t tsh = p->tshift, tmask = (1u << tsh) - 1;
+	const float2 *tq = (const float2 *)p->tq2;
+	const uint32_t L = (uint32_t)L1 * L23;
+	const float xL = 2.0f / (float)L;
 	const float2 *A = scratch + hg.sa;
 	float2 *B = scratch + hg.sb;
 	if (!tk_wait(done_a, (int)hg.na, err, failed, spin_limit))
@@ -562,11 +582,11 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 		if (k1 >= L1 || n3 >= L3)
 			return;
 		const uint32_t m = (uint32_t)n3 * ((uint32_t)k1 + (uint32_t)L1 * (uint32_t)j);
-		const float2 b = cmul(__ldg(thi + (m >> tsh)), __ldg(tlo + (m & tmask)));
+		const float2 b = tk_wm(m, L, xL);
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
 		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
 	};
-	tile_chain<false, Rows>(&p->c2, (const float2 *)p->tw2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(&p->c2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done_b);
 }
@@ -618,7 +638,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 			__stcs(o2 + m, conjf2(v));
 		}
 	};
-	tile_chain<false, Rows>(&p->c3, (const float2 *)p->tw3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(&p->c3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 }
 
