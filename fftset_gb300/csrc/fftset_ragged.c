@@ -200,6 +200,10 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			const fgk_plan *pl = f->rg_tuned && f->rg_dmem ? &f->rg_plan : &f->rp;
 			const uint32_t tg = f->rg_tuned ? f->rg_tg : fsr_item_threads(pl);
 			uint32_t G = (uint32_t)fgk_tasks_threads(rb->wide) / tg;
+			if (!pl->fwd.code) { /* tiles take chains of at most 15 stages */
+				rc = FFTSET_E_UNSUPPORTED;
+				goto fail;
+			}
 			if (G * fsr_slots(L) > (uint32_t)fgk_tasks_slots())
 				G = (uint32_t)fgk_tasks_slots() / fsr_slots(L);
 			plans[nplans] = *pl;
@@ -214,10 +218,21 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			if ((rc = fs_ensure_threestep(fs, f)) != 0)
 				goto fail;
 			p3 = &f->p3;
+			if (!p3->c1.code || !p3->c2.code || !p3->c3.code) {
+				rc = FFTSET_E_UNSUPPORTED;
+				goto fail;
+			}
 			for (k = i; k < j; k++) {
 				fgk_huge *h = &huges[nhuge++];
 				const size_t span = ((size_t)L + 15) & ~(size_t)15;
 				h->p3 = p3->dev;
+				h->L1 = p3->L1;
+				h->L2 = p3->L2;
+				h->L3 = p3->L3;
+				h->reserved = 0;
+				h->code1 = p3->c1.code;
+				h->code2 = p3->c2.code;
+				h->code3 = p3->c3.code;
 				h->in_off = in_offsets[order[k].idx];
 				h->out_off = out_offsets[order[k].idx];
 				h->sa = scratch_f2;
@@ -236,13 +251,18 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			L1 = f->p4.L1;
 			L2 = f->p4.L2;
 			/* tiles of 16 or more lanes (the task kernel's Rows layout) */
-			if ((L1 << 4) > (uint32_t)fgk_tasks_points() || (L2 << 4) > (uint32_t)fgk_tasks_points()) {
+			if ((L1 << 4) > (uint32_t)fgk_tasks_points() || (L2 << 4) > (uint32_t)fgk_tasks_points() ||
+			    !f->p4.c1.code || !f->p4.c2.code) {
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
 			}
 			for (k = i; k < j; k++) {
 				fgk_big *b = &bigs[nbig++];
 				b->p4 = f->p4.dev;
+				b->L1 = L1;
+				b->L2 = L2;
+				b->code1 = f->p4.c1.code;
+				b->code2 = f->p4.c2.code;
 				b->in_off = in_offsets[order[k].idx];
 				b->out_off = out_offsets[order[k].idx];
 				b->scratch_off = scratch_f2;

@@ -27,6 +27,9 @@ typedef struct fgk_stage {
 
 typedef struct fgk_chain {
 	uint32_t  nstages;
+	uint32_t  reserved;
+	uint64_t  code; /* nstages in bits 0-3, radix of stage s minus 1 in bits 4s+4 .. 4s+7 (chains
+	                   of at most 15 stages; 0 otherwise): the whole chain in one load */
 	fgk_stage st[FGK_MAX_STAGES];
 } fgk_chain;
 
@@ -144,6 +147,8 @@ int fgk_launch_spectrum_natural(const float *kern, const int32_t *kidx, int kvw,
  * wait for every A tile of the item, C tiles for every B tile. */
 typedef struct fgk_huge {
 	const struct fgk_plan3 *p3;             /* device copy of the item's plan */
+	uint32_t                L1, L2, L3, reserved;
+	uint64_t                code1, code2, code3; /* the passes' chains (fgk_chain.code) */
 	uint64_t                in_off, out_off; /* floats from the batch's base pointers */
 	uint64_t                sa, sb;          /* float2 offsets of its A and B scratch */
 	uint32_t                na, nb;          /* A tiles, B tiles */
@@ -152,6 +157,8 @@ typedef struct fgk_huge {
 
 typedef struct fgk_big {
 	const struct fgk_plan4 *p4;            /* device copy of the item's four-step plan */
+	uint32_t                L1, L2;
+	uint64_t                code1, code2;    /* the COLS / ROWS chains (fgk_chain.code) */
 	uint64_t                in_off, out_off; /* floats from the batch's base pointers */
 	uint64_t                scratch_off;     /* float2 offset of the item's L1 x L2 scratch */
 	uint32_t                ncols;           /* COLS tiles */

@@ -138,6 +138,10 @@ static void fill_chain(fgk_chain *ch, const uint32_t *rad, uint32_t n, uint32_t 
 {
 	uint32_t s, ns = 1;
 	ch->nstages = n;
+	ch->reserved = 0;
+	ch->code = n <= 15 ? n : 0;
+	for (s = 0; s < n && n <= 15; s++)
+		ch->code |= (uint64_t)(rad[s] - 1) << (4 * s + 4);
 	for (s = 0; s < n; s++) {
 		ch->st[s].radix = rad[s];
 		ch->st[s].ns = ns;

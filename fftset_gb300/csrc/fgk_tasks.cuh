@@ -22,7 +22,7 @@
  * Rows layout below conflict-free.
  *
  * A ROWS task waits for all COLS tasks of its item: each COLS task bumps the
- * item's counter after its stores are visible (threadfence), and a ROWS task
+ * item's counter with a gpu-scope release add after a barrier, and a ROWS task
  * spins on it with a bounded wait (on timeout it raises the error flag and
  * skips the tile). Tasks are claimed in list order from an atomic counter,
  * and the host lists every COLS task of an item before its ROWS tasks, so a
@@ -250,38 +250,40 @@ __device__ __forceinline__ void lane_single(Ld &&ld, St &&st, int ls, int tid, i
  * stage is done (all of its reads have returned). Threads with active ==
  * false only take part in the barriers. */
 template <bool JF, class AD, class Ld, class St, class After>
-__device__ __forceinline__ void tile_chain(const fgk_chain *ch, int Lp, int ls, float2 *A,
-                                           float2 *B, int tid, int T, bool active, Ld &&ld, St &&st,
-                                           After &&after_first)
+__device__ __forceinline__ void tile_chain(uint64_t code, int Lp, int ls, float2 *A, float2 *B, int tid, int T,
+                                           bool active, Ld &&ld, St &&st, After &&after_first)
 {
+	/* the chain comes packed in one word (fgk_chain.code) from the task's
+	 * descriptor: no stage reads global memory for its radix */
 	const AD ad{ls};
-	const int n = (int)ch->nstages;
+	const int n = (int)(code & 15);
+	const int r0 = (int)((code >> 4) & 15) + 1;
 	if (n == 1) {
 		if (active)
-			FGKR_RADIX_SWITCH(ch->st[0].radix, (lane_single<R_>(ld, st, ls, tid, T)));
+			FGKR_RADIX_SWITCH(r0, (lane_single<R_>(ld, st, ls, tid, T)));
 		__syncthreads();
 		after_first();
 		return;
 	}
-	if (active) {
-		const fgk_stage st0 = ch->st[0];
-		FGKR_RADIX_SWITCH(st0.radix, (lane_first<R_>(ld, A, Lp, ls, tid, T, ad)));
-	}
+	if (active)
+		FGKR_RADIX_SWITCH(r0, (lane_first<R_>(ld, A, Lp, ls, tid, T, ad)));
 	__syncthreads();
 	after_first();
 	float2 *src = A, *dst = B;
+	int ns = r0;
 	for (int s = 1; s < n - 1; s++) {
-		const fgk_stage sm = ch->st[s];
+		const int r = (int)((code >> (4 * s + 4)) & 15) + 1;
 		if (active)
-			FGKR_RADIX_SWITCH(sm.radix, (lane_stage<R_>(src, dst, Lp, ls, (int)sm.ns, tid, T, ad)));
+			FGKR_RADIX_SWITCH(r, (lane_stage<R_>(src, dst, Lp, ls, ns, tid, T, ad)));
 		__syncthreads();
+		ns *= r;
 		float2 *t = src;
 		src = dst;
 		dst = t;
 	}
 	if (active) {
-		const fgk_stage sl = ch->st[n - 1];
-		FGKR_RADIX_SWITCH(sl.radix, (lane_last<R_, JF>(src, st, Lp, ls, tid, T, ad)));
+		const int rl = (int)((code >> (4 * n)) & 15) + 1;
+		FGKR_RADIX_SWITCH(rl, (lane_last<R_, JF>(src, st, Lp, ls, tid, T, ad)));
 	}
 }
 
@@ -307,21 +309,23 @@ __device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int 
 			}
 			__nanosleep(256);
 		}
-		__threadfence();
+		/* no fence: the acquire load, then the barrier, order every
+		 * thread's later reads after the counted tiles' stores */
 		*failed = f;
 	}
 	__syncthreads();
 	return !*failed;
 }
 
-/* A tile's scratch stores, then one gpu-scope release of its count */
+/* A tile's scratch stores, a barrier, then one gpu-scope release add of its
+ * count (cumulative: it publishes the whole CTA's stores). The release add
+ * replaces a full fence plus a relaxed add, which held the CTA's last
+ * barrier until the fence drained. */
 __device__ __forceinline__ void tk_signal(int *ctr)
 {
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		__threadfence();
-		atomicAdd(ctr, 1);
-	}
+	if (threadIdx.x == 0)
+		asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(ctr) : "memory");
 }
 
 /* v times bin m of the product's natural-order spectrum */
@@ -381,7 +385,7 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
 			__stcs(y2 + k, conjf2(v));
 		}
 	};
-	tile_chain<false, Pad>(&pl->fwd, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
+	tile_chain<false, Pad>(pl->fwd.code, L, 0, buf0, buf0 + rslots(L), tid, T, active, ld, st,
 	                       pre);
 }
 
@@ -394,7 +398,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
                                           float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
-	const int L1 = (int)p->L1, L2 = (int)p->L2;
+	const int L1 = (int)bg.L1, L2 = (int)bg.L2;
 	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
 	const int ls = (int)bg.ls1;
 	const int ls2 = (int)bg.ls2, lm2 = (1 << ls2) - 1;
@@ -432,7 +436,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 		__stcg(S + ((((uint32_t)(k1 >> ls2) * (uint32_t)L2 + (uint32_t)n2) << ls2) + (uint32_t)(k1 & lm2)),
 		       cmul(v, w));
 	};
-	tile_chain<true, Rows>(&p->c1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<true, Rows>(bg.code1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                       (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
@@ -445,7 +449,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
                                           float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
-	const int L1 = (int)p->L1, L2 = (int)p->L2;
+	const int L1 = (int)bg.L1, L2 = (int)bg.L2;
 	const uint32_t L = (uint32_t)L1 * (uint32_t)L2;
 	const int ls = (int)bg.ls2, nl = 1 << ls;
 	const int k1base = (int)(tk.a << ls);
@@ -492,7 +496,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 		for (uintptr_t a = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)tid * 128; a + 128 <= b1; a += (uintptr_t)T * 128)
 			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
 	};
-	tile_chain<false, Rows>(&p->c2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
+	tile_chain<false, Rows>(bg.code2, L2, ls, smem, smem + TK_SLOTS, tid, T, true, ld, st,
 	                        [&] {
 		                        discard();
 		                        pre();
@@ -508,15 +512,15 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
                                         float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
-	const int L1 = (int)p->L1, L3 = (int)p->L3;
-	const uint32_t L23 = p->L2 * p->L3, L = (uint32_t)L1 * L23;
+	const int L1 = (int)hg.L1, L3 = (int)hg.L3;
+	const uint32_t L23 = hg.L2 * hg.L3, L = (uint32_t)L1 * L23;
 	const int cbase = (int)(tk.a << 4);
 	const float inv3 = 1.0f / (float)L3;
 	const float *x = in_base + hg.in_off;
 	const float2 *x2 = reinterpret_cast<const float2 *>(x);
 	const float2 *ma = (const float2 *)p->ma, *mb = (const float2 *)p->mb, *mc = (const float2 *)p->mc;
 	const float2 *tq = (const float2 *)p->tq1;
-	const uint32_t L12 = (uint32_t)L1 * p->L2;
+	const uint32_t L12 = (uint32_t)L1 * hg.L2;
 	const float x12 = 2.0f / (float)L12;
 	float2 *A = scratch + hg.sa;
 	auto ld = [&](int n1, int lane) {
@@ -546,7 +550,7 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : b;
 		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
 	};
-	tile_chain<false, Rows>(&p->c1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(hg.code1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done);
 }
@@ -560,7 +564,7 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
                                         Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
-	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const int L1 = (int)hg.L1, L2 = (int)hg.L2, L3 = (int)hg.L3;
 	const uint32_t L23 = (uint32_t)L2 * L3;
 	const int k1g = (int)(tk.a / hg.nb3);
 	const int k1b = k1g * 4, n3b = (int)(tk.a - (uint32_t)k1g * hg.nb3) * 4;
@@ -586,7 +590,7 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
 		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
 	};
-	tile_chain<false, Rows>(&p->c2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(hg.code2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 	tk_signal(done_b);
 }
@@ -599,7 +603,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
                                         float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
-	const int L1 = (int)p->L1, L2 = (int)p->L2, L3 = (int)p->L3;
+	const int L1 = (int)hg.L1, L2 = (int)hg.L2, L3 = (int)hg.L3;
 	const uint32_t L = (uint32_t)L1 * L2 * L3;
 	const int k2 = (int)(tk.a / hg.nc1);
 	const int k1b = (int)(tk.a - (uint32_t)k2 * hg.nc1) * 16;
@@ -638,7 +642,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 			__stcs(o2 + m, conjf2(v));
 		}
 	};
-	tile_chain<false, Rows>(&p->c3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
+	tile_chain<false, Rows>(hg.code3, L3, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 }
 
