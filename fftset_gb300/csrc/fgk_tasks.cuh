@@ -317,15 +317,14 @@ __device__ __forceinline__ bool tk_wait(const int *ctr, int need, int *err, int 
 	return !*failed;
 }
 
-/* A tile's scratch stores, a barrier, then one gpu-scope release add of its
- * count (cumulative: it publishes the whole CTA's stores). The release add
- * replaces a full fence plus a relaxed add, which held the CTA's last
- * barrier until the fence drained. */
-__device__ __forceinline__ void tk_signal(int *ctr)
+/* A tile's count: after the task loop's barrier that follows the tile (so
+ * after every thread's scratch stores), thread 0 makes one gpu-scope
+ * release add (cumulative: it publishes the whole CTA's stores). Tiles that
+ * count return their counter to the loop; the loop's barrier is the only
+ * one, and a release add takes no full fence. */
+__device__ __forceinline__ void tk_release(int *ctr)
 {
-	__syncthreads();
-	if (threadIdx.x == 0)
-		asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(ctr) : "memory");
+	asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(ctr) : "memory");
 }
 
 /* v times bin m of the product's natural-order spectrum */
@@ -394,7 +393,7 @@ __device__ __forceinline__ void task_small(const fgk_task &tk, const fgk_plan *_
  * (k1, n2) at ((k1 >> ls2) L2 + n2) 2^ls2 + (k1 & (2^ls2 - 1)), so a ROWS
  * tile reads one contiguous block with its lanes fastest. */
 template <bool inverse, bool freq, class Pre>
-__device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg, const float *in_base,
+__device__ __forceinline__ int *task_cols(const fgk_task &tk, const fgk_big &bg, const float *in_base,
                                           float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan4 *p = bg.p4;
@@ -438,7 +437,7 @@ __device__ __forceinline__ void task_cols(const fgk_task &tk, const fgk_big &bg,
 	};
 	tile_chain<true, Rows>(bg.code1, L1, ls, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                       (int)blockDim.x, true, ld, st, pre);
-	tk_signal(done);
+	return done;
 }
 
 /* ROWS: rows k1base .. k1base + 2^ls2 - 1 of the scratch, DFTs of length L2
@@ -508,7 +507,7 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
  * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
  * A[k1][c] (a warp's 16 lanes write one 128-byte segment). */
 template <bool inverse, bool freq, class Pre>
-__device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
+__device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
                                         float2 *scratch, int *done, float2 *smem, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
@@ -552,14 +551,14 @@ __device__ __forceinline__ void task_pa(const fgk_task &tk, const fgk_huge &hg, 
 	};
 	tile_chain<false, Rows>(hg.code1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
-	tk_signal(done);
+	return done;
 }
 
 /* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
  * n2 from A (32-byte segments), times w_L^{n3 (k1 + L1 k2)} =
  * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
 template <bool inverse, bool freq, class Pre>
-__device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
+__device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
                                         int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
                                         Pre &&pre)
 {
@@ -574,7 +573,7 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	const float2 *A = scratch + hg.sa;
 	float2 *B = scratch + hg.sb;
 	if (!tk_wait(done_a, (int)hg.na, err, failed, spin_limit))
-		return;
+		return nullptr;
 	auto ld = [&](int n2, int lane) {
 		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
 		if (k1 >= L1 || n3 >= L3)
@@ -592,7 +591,7 @@ __device__ __forceinline__ void task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	};
 	tile_chain<false, Rows>(hg.code2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
-	tk_signal(done_b);
+	return done_b;
 }
 
 /* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from B (128-byte segments),
@@ -688,20 +687,21 @@ __global__ void __launch_bounds__(THREADS, MINB)
 		if (c >= ntasks)
 			break;
 		const fgk_task tk = next_task;
+		int *count = nullptr; /* the tile's counter, released after the barrier below */
 		if (threadIdx.x == 0)
 			ahead = (uint32_t)atomicAdd(counters, 1);
 		if (tk.kind == FGK_TASK_SMALL)
 			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem, pre);
 		else if (tk.kind == FGK_TASK_COLS)
-			task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
+			count = task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_ROWS)
 			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, spin_limit,
 			                         prod, smem, &failed, pre);
 		else if (tk.kind == FGK_TASK_PA)
-			task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
+			count = task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
 		else if (tk.kind == FGK_TASK_PB)
-			task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref, hcounters + 2 * tk.ref + 1, err,
-			                       spin_limit, smem, &failed, pre);
+			count = task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref,
+			                               hcounters + 2 * tk.ref + 1, err, spin_limit, smem, &failed, pre);
 		else
 			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, spin_limit,
 			                       prod, smem, &failed, pre);
@@ -724,6 +724,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
 			cur = ahead;
 		}
 		__syncthreads(); /* buffers are reused by the next task */
+		if (threadIdx.x == 0 && count)
+			tk_release(count);
 	}
 }
 
