@@ -224,7 +224,8 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			}
 			for (k = i; k < j; k++) {
 				fgk_huge *h = &huges[nhuge++];
-				const size_t span = ((size_t)L + 15) & ~(size_t)15;
+				/* each scratch area in 4 x 4 blocks: L2 ceil(L1/4) ceil(L3/4) x 16 */
+				const size_t span = (size_t)p3->L2 * ((p3->L1 + 3) / 4) * ((p3->L3 + 3) / 4) * 16;
 				h->p3 = p3->dev;
 				h->L1 = p3->L1;
 				h->L2 = p3->L2;

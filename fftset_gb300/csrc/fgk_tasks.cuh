@@ -503,9 +503,26 @@ __device__ __forceinline__ void task_rows(const fgk_task &tk, const fgk_big &bg,
 }
 
 /* ---- three-level items (fgk_plan3): passes A, B, C ------------------- */
+/* The two scratch areas are laid out in blocks of 4 k1 x 4 n3 (128 bytes),
+ * L1q = ceil(L1/4) and L3q = ceil(L3/4) blocks along k1 and n3:
+ *   A (k1, n2, n3) in block ((n2 L3q + n3/4) L1q + k1/4), at (k1%4) 4 + n3%4;
+ *   B (k2, n3, k1) in block ((k2 L1q + k1/4) L3q + n3/4), at (n3%4) 4 + k1%4.
+ * A pass-B tile (4 k1 x 4 n3 lanes) then reads one whole block of A per n2
+ * and writes one whole block of B per k2; a pass-A store of 16 adjacent n3
+ * fills four 32-byte sectors, and a pass-C load of 16 adjacent k1 reads four
+ * whole sectors. */
+__device__ __forceinline__ uint32_t tk_blk_a(uint32_t k1, uint32_t n2, uint32_t n3, uint32_t L1q, uint32_t L3q)
+{
+	return (((n2 * L3q + (n3 >> 2)) * L1q + (k1 >> 2)) << 4) + ((k1 & 3) << 2) + (n3 & 3);
+}
+__device__ __forceinline__ uint32_t tk_blk_b(uint32_t k2, uint32_t n3, uint32_t k1, uint32_t L1q, uint32_t L3q)
+{
+	return (((k2 * L1q + (k1 >> 2)) * L3q + (n3 >> 2)) << 4) + ((n3 & 3) << 2) + (k1 & 3);
+}
+
 /* A: 16 adjacent columns c = n2 L3 + n3, DFT_L1 over n1 straight from the
  * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
- * A[k1][c] (a warp's 16 lanes write one 128-byte segment). */
+ * the blocked A. */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
                                         float2 *scratch, int *done, float2 *smem, Pre &&pre)
@@ -539,6 +556,7 @@ __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, 
 			return n < ((L + 1) >> 1) ? conjf2(__ldcs(x2 + 2 * n)) : __ldcs(x2 + 2 * (L - 1 - n) + 1);
 		return conjf2(__ldcs(x2 + n));
 	};
+	const uint32_t L1q = (uint32_t)(L1 + 3) >> 2, L3q = hg.nb3;
 	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
 		const uint32_t c = (uint32_t)(cbase + lane);
 		if (c >= L23)
@@ -547,7 +565,8 @@ __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, 
 		const uint32_t m = (uint32_t)n2 * (uint32_t)j;
 		const float2 b = tk_wm(m, L12, x12);
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n2 * (uint32_t)q)) : b;
-		__stcg(A + (uint32_t)(j + q * nbf) * L23 + c, cmul(v, w));
+		__stcg(A + tk_blk_a((uint32_t)(j + q * nbf), (uint32_t)n2, c - (uint32_t)n2 * (uint32_t)L3, L1q, L3q),
+		       cmul(v, w));
 	};
 	tile_chain<false, Rows>(hg.code1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
@@ -555,8 +574,9 @@ __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, 
 }
 
 /* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
- * n2 from A (32-byte segments), times w_L^{n3 (k1 + L1 k2)} =
- * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into B[(k2 L3 + n3) L1 + k1]. */
+ * n2 from the blocked A (one block per n2), times w_L^{n3 (k1 + L1 k2)} =
+ * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into the blocked B (one block per
+ * k2). */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
                                         int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
@@ -574,11 +594,12 @@ __device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	float2 *B = scratch + hg.sb;
 	if (!tk_wait(done_a, (int)hg.na, err, failed, spin_limit))
 		return nullptr;
+	const uint32_t L1q = hg.nb / hg.nb3, L3q = hg.nb3;
 	auto ld = [&](int n2, int lane) {
 		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
 		if (k1 >= L1 || n3 >= L3)
 			return make_float2(0.f, 0.f);
-		return __ldcg(A + (uint32_t)k1 * L23 + (uint32_t)n2 * L3 + n3);
+		return __ldcg(A + tk_blk_a((uint32_t)k1, (uint32_t)n2, (uint32_t)n3, L1q, L3q));
 	};
 	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
 		const int k1 = k1b + (lane >> 2), n3 = n3b + (lane & 3);
@@ -587,15 +608,16 @@ __device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, 
 		const uint32_t m = (uint32_t)n3 * ((uint32_t)k1 + (uint32_t)L1 * (uint32_t)j);
 		const float2 b = tk_wm(m, L, xL);
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
-		__stcg(B + ((uint32_t)(j + q * nbf) * L3 + n3) * (uint32_t)L1 + k1, cmul(v, w));
+		__stcg(B + tk_blk_b((uint32_t)(j + q * nbf), (uint32_t)n3, (uint32_t)k1, L1q, L3q), cmul(v, w));
 	};
 	tile_chain<false, Rows>(hg.code2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
 	return done_b;
 }
 
-/* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from B (128-byte segments),
- * into X[k1 + L1 k2 + L1 L2 k3] (the modulation's final step fused). */
+/* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from the blocked B (four
+ * 32-byte sectors per n3), into X[k1 + L1 k2 + L1 L2 k3] (the modulation's
+ * final step fused). */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
                                         const int *done_b, int *err, uint32_t spin_limit, const fgk_product &prod,
@@ -612,11 +634,12 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 	const float2 *oa = (const float2 *)p->oa, *ob = (const float2 *)p->ob, *oc = (const float2 *)p->oc;
 	if (!tk_wait(done_b, (int)hg.nb, err, failed, spin_limit))
 		return;
+	const uint32_t L1q = hg.nb / hg.nb3, L3q = hg.nb3;
 	auto ld = [&](int n3, int lane) {
 		const int k1 = k1b + lane;
 		if (k1 >= L1)
 			return make_float2(0.f, 0.f);
-		return __ldcg(B + ((uint32_t)k2 * L3 + n3) * (uint32_t)L1 + k1);
+		return __ldcg(B + tk_blk_b((uint32_t)k2, (uint32_t)n3, (uint32_t)k1, L1q, L3q));
 	};
 	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
 		const int k1 = k1b + lane;
