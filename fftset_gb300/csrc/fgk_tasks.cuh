@@ -46,15 +46,15 @@ namespace fgk {
 #ifndef FGKT_POINTS
 #define FGKT_POINTS 4096 /* points of a tile */
 #endif
-/* Two CTA shapes, chosen per task list: narrow, 128 threads and three CTAs
- * per SM (three tiles in flight per SM, 168 registers a thread), for lists
- * of items up to 65536 bins (the ragged mix: 1.998 against 2.106 ms for the
- * 20000-item batch); wide, 256 threads and two CTAs per SM (128 registers),
- * for lists with three-level items (the 15,728,640-bin transform: 0.737
- * against 0.786 ms). Both shapes fit the 128-register budget with no
- * spills; at three CTAs of 256 threads (80 registers) the kernel spilled. */
+/* Two CTA shapes, chosen per task list, both three CTAs (three tiles) per
+ * SM: narrow, 128 threads (up to 168 registers a thread, no spills), for
+ * lists of items up to 65536 bins (the 20000-item ragged mix: 1.757 ms
+ * against 1.851 on two wide CTAs per SM and 1.90 on three); wide, 256
+ * threads (80 registers, a few hundred bytes of spills), for lists with
+ * three-level items (the 15,728,640-bin forward + inverse: 0.604 ms against
+ * 0.641 on two wide CTAs per SM, with no spills, and 0.684 narrow). */
 constexpr int TK_THREADS_NARROW = 128, TK_CTAS_NARROW = 3;
-constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 2;
+constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 3;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
 constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
 
