@@ -130,6 +130,8 @@ int fftset_init(struct fftset *fc)
 	fs->stream = fs->own_stream;
 	fs->spin_limit = 1u << 22; /* about a second */
 	fs->task_shape = -1;
+	fs->srv.idle_polls = FS_SERVE_IDLE_POLLS;
+	fs->srv.last_v = -1;
 	fs->blocking = 1;
 	fs->layout_vw = 4;
 	fs->device = dev;
@@ -147,6 +149,11 @@ void fftset_destroy(struct fftset *fc)
 	if (fs == NULL)
 		return;
 	cudaStreamSynchronize(fs->stream);
+	fs_serve_stop(fs);
+	if (fs->srv.stream)
+		cudaStreamDestroy(fs->srv.stream);
+	if (fs->srv.map)
+		cudaFreeHost(fs->srv.map);
 	for (p = fs->first; p != NULL; p = n) {
 		n = p->next;
 		for (i = 0; i < FS_TASK_LISTS; i++)
@@ -859,6 +866,155 @@ static int fs_exec_pipelined(const struct fftset_fft *f, int op, float *out, siz
 	return rc;
 }
 
+/* ---- the call service ----------------------------------------------------
+ * Blocking single calls on device buffers of a compiled variant that has a
+ * call service (fgk.h) are answered by one resident CTA instead of a launch
+ * and a stream synchronisation: the request goes into a pinned, mapped page,
+ * the doorbell is a sequence number, and the call returns when the CTA has
+ * published that number in `reply` (its output stores released before it).
+ * A launch of the service is made only when the same (plan, variant) is
+ * called twice in a row; it exits on its own after FS_SERVE_IDLE_POLLS idle
+ * polls, and every host wait here is bounded, ending in a wait for the
+ * service's stream and, if the request is still pending, a new launch. */
+#define FS_SERVE_SPIN (1u << 26) /* host polls of `reply` before checking on the service the slow way */
+
+static uint64_t fs_ld(const volatile uint64_t *p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
+
+static int fs_serve_init(struct fs_impl *fs)
+{
+	struct fs_serve *s = &fs->srv;
+	char *h = NULL, *d = NULL;
+	if (cudaHostAlloc((void **)&h, 4096, cudaHostAllocMapped) != cudaSuccess ||
+	    cudaHostGetDevicePointer((void **)&d, h, 0) != cudaSuccess ||
+	    cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+		cudaGetLastError();
+		if (h)
+			cudaFreeHost(h);
+		s->stream = NULL;
+		return -1;
+	}
+	memset(h, 0, 4096);
+	s->map = h;
+	/* one 128-byte line per word */
+	s->bell = (volatile uint64_t *)(h + 0);
+	s->reply = (volatile uint64_t *)(h + 128);
+	s->state = (volatile uint64_t *)(h + 256);
+	s->req = (fgk_serve_req *)(h + 384);
+	s->dev.bell = (const volatile uint64_t *)(d + 0);
+	s->dev.reply = (volatile uint64_t *)(d + 128);
+	s->dev.state = (volatile uint64_t *)(d + 256);
+	s->dev.req = (const fgk_serve_req *)(d + 384);
+	return 0;
+}
+
+/* a new launch for (f, v) that has seen every request before `seen` */
+static int fs_serve_launch(struct fs_impl *fs, const struct fftset_fft *f, int v, uint64_t seen)
+{
+	struct fs_serve *s = &fs->srv;
+	const uint64_t id = ++s->id;
+	int rc;
+	__atomic_store_n(s->state, id, __ATOMIC_RELEASE);
+	rc = fgk_launch_static_serve(&f->vp[v], v, s->dev, seen, id, s->idle_polls, s->stream);
+	if (rc != 0) {
+		cudaGetLastError();
+		__atomic_store_n(s->state, 0, __ATOMIC_RELEASE);
+		return -1;
+	}
+	s->f = f;
+	s->v = v;
+	return 0;
+}
+
+/* the live launch, if any, leaves: a request with op -1, then its stream */
+void fs_serve_stop(struct fs_impl *fs)
+{
+	struct fs_serve *s = &fs->srv;
+	if (!s->map || !s->stream)
+		return;
+	if (fs_ld(s->state) == s->id && s->id) {
+		s->req->op = -1;
+		__atomic_store_n(s->bell, ++s->seq, __ATOMIC_SEQ_CST);
+	}
+	cudaStreamSynchronize(s->stream);
+	cudaGetLastError();
+	s->f = NULL;
+}
+
+/* -1: not taken (the caller runs the call the usual way), else the call's
+ * FFTSET status */
+static int fs_serve_call(const struct fftset_fft *f, int v, int op, float *out, const float *in, const float *kern)
+{
+	struct fs_impl *fs = f->fs;
+	struct fs_serve *s = &fs->srv;
+	uint64_t seq;
+	unsigned relaunch = 0;
+	uint32_t polls;
+	cudaError_t e;
+	if (!s->idle_polls || s->broken || !fgk_static_serve_ok(f->rp.modulation, f->lfft, v, op))
+		return -1;
+	pthread_mutex_lock(&fs->lock);
+	if (s->last_f != f || s->last_v != v) {
+		/* a launch pays off from the second call of the same kind */
+		s->last_f = f;
+		s->last_v = v;
+		pthread_mutex_unlock(&fs->lock);
+		return -1;
+	}
+	if (!s->map && fs_serve_init(fs) != 0) {
+		s->broken = 1;
+		pthread_mutex_unlock(&fs->lock);
+		return -1;
+	}
+	/* a blocking call runs after the work already queued on the stream */
+	if ((e = cudaStreamSynchronize(fs->stream)) != cudaSuccess) {
+		pthread_mutex_unlock(&fs->lock);
+		return fs_cuda(fs, e);
+	}
+	if (!(s->f == f && s->v == v && s->id && fs_ld(s->state) == s->id)) {
+		fs_serve_stop(fs);
+		if (fs_serve_launch(fs, f, v, s->seq) != 0) {
+			s->broken = 1;
+			pthread_mutex_unlock(&fs->lock);
+			return -1;
+		}
+	}
+	s->req->op = op;
+	s->req->in = in;
+	s->req->out = out;
+	s->req->kern = kern;
+	seq = ++s->seq;
+	__atomic_store_n(s->bell, seq, __ATOMIC_SEQ_CST);
+	__atomic_thread_fence(__ATOMIC_SEQ_CST);
+	for (polls = 0;; polls++) {
+		if (fs_ld(s->reply) == seq)
+			break;
+		if (fs_ld(s->state) != s->id || polls >= FS_SERVE_SPIN) {
+			/* the launch left (or stopped answering): once its stream is
+			 * done, either it answered on its way out or the request is
+			 * still pending and a new launch takes it */
+			if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) {
+				s->broken = 1;
+				pthread_mutex_unlock(&fs->lock);
+				return fs_cuda(fs, e);
+			}
+			if (fs_ld(s->reply) == seq)
+				break;
+			if (++relaunch > 2 || fs_serve_launch(fs, f, v, seq - 1) != 0) {
+				/* the request is void now (no launch is alive): run it the
+				 * usual way */
+				s->broken = 1;
+				s->f = NULL;
+				pthread_mutex_unlock(&fs->lock);
+				return -1;
+			}
+			polls = 0;
+		}
+	}
+	s->served++;
+	pthread_mutex_unlock(&fs->lock);
+	return FFTSET_OK;
+}
+
 /* Runs op on `count` blocks. Buffers of any memory kind. */
 static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_stride, const float *in,
                    size_t in_stride, const float *kern, unsigned count)
@@ -890,6 +1046,11 @@ static int fs_exec(const struct fftset_fft *f, int op, float *out, size_t out_st
 	const struct fs_ptrinfo pin = fs_classify(in), pout = fs_classify(out), pkern = fs_classify(kern);
 
 	if (pin.dev && pout.dev && pkern.dev) {
+		if (fs->blocking && count == 1 && !f->fourstep) {
+			rc = fs_serve_call(f, fs_pick_variant(f, op, 1), op, out, in, kern);
+			if (rc >= 0)
+				return rc;
+		}
 		rc = fs_launch(f, op, out, in, kern, count, in_stride, out_stride);
 		if (rc < 0)
 			return fs_latch(fs, -rc, 0);
@@ -1151,6 +1312,26 @@ int fftset__test_set_spin_limit(struct fftset *fc, unsigned polls)
 		return FFTSET_E_INVALID;
 	fs->spin_limit = polls;
 	return FFTSET_OK;
+}
+
+int fftset__test_set_call_service(struct fftset *fc, unsigned idle_polls)
+{
+	struct fs_impl *fs = fs_of(fc);
+	if (!fs)
+		return FFTSET_E_INVALID;
+	pthread_mutex_lock(&fs->lock);
+	fs_serve_stop(fs);
+	fs->srv.idle_polls = idle_polls;
+	fs->srv.broken = 0;
+	fs->srv.last_f = NULL;
+	pthread_mutex_unlock(&fs->lock);
+	return FFTSET_OK;
+}
+
+unsigned long long fftset__test_served_calls(struct fftset *fc)
+{
+	struct fs_impl *fs = fs_of(fc);
+	return fs ? fs->srv.served : 0;
 }
 
 int fftset__test_set_task_shape(struct fftset *fc, int shape)

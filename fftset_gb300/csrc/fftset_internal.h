@@ -71,6 +71,29 @@ struct fftset_fft {
 
 #define FS_NSTAGE 5 /* staging buffers: input, output, kernel, four-step work, adjoint scratch */
 #define FS_PIPE   3 /* streams of the host-buffer chunk pipeline */
+/* doorbell polls (about 0.8 us each over NVLink-C2C) before an idle call
+ * service exits: a caller that waits longer than this between blocking
+ * calls pays one launch on its next call */
+#define FS_SERVE_IDLE_POLLS 64
+
+/* The call service (fgk.h, fgk_launch_static_serve): one resident CTA that
+ * runs blocking single calls of a compiled variant without a launch each. */
+struct fs_serve {
+	void                  *map;   /* pinned, mapped page: the words and the request */
+	volatile uint64_t     *bell, *reply, *state;
+	fgk_serve_req         *req;
+	fgk_serve_words        dev;   /* the same, as device addresses */
+	cudaStream_t           stream;
+	const struct fftset_fft *f;   /* what the live launch serves (f, v) */
+	int                    v;
+	uint64_t               seq;   /* last request sequence number issued */
+	uint64_t               id;    /* id of the latest launch (0: none yet) */
+	const struct fftset_fft *last_f; /* the previous eligible call's (f, v): a */
+	int                    last_v;   /* launch is only worth it on a repeat */
+	uint32_t               idle_polls; /* doorbell polls before an idle CTA exits; 0: off */
+	int                    broken;     /* a failure turned the service off */
+	unsigned long long     served;     /* requests answered */
+};
 
 struct fs_impl {
 	cudaStream_t       stream;
@@ -97,6 +120,7 @@ struct fs_impl {
 	size_t             stage_bytes[FS_NSTAGE];
 	cudaStream_t       pipe[FS_PIPE]; /* host-buffer chunk pipeline (fs_exec) */
 	cudaEvent_t        pipe_ev;
+	struct fs_serve    srv;
 };
 
 
@@ -105,6 +129,8 @@ int  fs_latch(struct fs_impl *fs, int code, int cuda_err);
 int  fs_cuda(struct fs_impl *fs, cudaError_t e);
 int  fs_is_device_ptr(const void *ptr);
 int  fs_check_flag(struct fs_impl *fs);
+/* the call service's live launch, if any, exits (fftset_host.c) */
+void fs_serve_stop(struct fs_impl *fs);
 /* four-step tables for a plan (built on demand for resident-size plans too) */
 int  fs_ensure_fourstep(struct fs_impl *fs, struct fftset_fft *f);
 /* three-level tables for a plan (sizes beyond 65536 bins), on demand */
@@ -153,6 +179,10 @@ void fftset__test_live_allocations(long *host, long *device);
  * (launches made afterwards), and a ragged batch without its tasks of one
  * kind (the tasks that wait on them then time out). */
 int  fftset__test_set_spin_limit(struct fftset *fc, unsigned polls);
+/* the call service's idle doorbell polls (0 turns it off; the default is
+ * FS_SERVE_IDLE_POLLS) and the number of requests it has served */
+int  fftset__test_set_call_service(struct fftset *fc, unsigned idle_polls);
+unsigned long long fftset__test_served_calls(struct fftset *fc);
 /* CTA shape of the task lists of later ragged creates: -1 chosen by the
  * list (wide when it holds three-level items), 0 narrow, 1 wide */
 int  fftset__test_set_task_shape(struct fftset *fc, int shape);

@@ -258,6 +258,40 @@ int fgk_static_ola_variant(uint32_t modulation, uint32_t L);
 int fgk_launch_static_ola(const fgk_plan *p, int v, const float *in, uint64_t n, uint32_t B, uint32_t span,
                           uint32_t nblocks, uint64_t nout, const float *kern, float *out, void *stream, int num_sms);
 
+/* The call service of a compiled variant (static_kernel_serve): one CTA
+ * that runs single transforms on request, with the variant's own stages and
+ * tables (so its results are the batched kernel's, bit for bit), without a
+ * launch per call. Requests and replies go through words in host-mapped
+ * memory (coherent over NVLink-C2C): the host writes the request, then the
+ * doorbell (a sequence number); thread 0 polls the doorbell, the CTA runs
+ * the op, and thread 0 publishes the sequence number in `reply` with a
+ * system-scope release once every output store is done. After idle_polls
+ * polls with nothing new the CTA writes 0 to `state`, reads the doorbell
+ * once more (after a system-scope fence) and exits unless it changed.
+ * All words are 64-bit, each in its own 128-byte line. */
+typedef struct fgk_serve_req {
+	int32_t      op; /* enum fgk_op (FORWARD, INVERSE, CONV or CORR) */
+	uint32_t     reserved;
+	const float *in;
+	float       *out;
+	const float *kern; /* CONV / CORR: the kernel buffer */
+} fgk_serve_req;
+
+typedef struct fgk_serve_words {
+	const volatile uint64_t *bell;  /* request sequence number (host writes) */
+	volatile uint64_t       *reply; /* last sequence number served (device writes) */
+	volatile uint64_t       *state; /* the live launch's id; 0 once it exits */
+	const fgk_serve_req     *req;   /* the pending request (host writes before the doorbell) */
+} fgk_serve_words;
+
+/* 1 when variant v of (modulation, L) has a call service that implements
+ * op (compiled variants without bulk-copy input) */
+int fgk_static_serve_ok(uint32_t modulation, uint32_t L, int v, int op);
+/* launches the service: `seen` is the last sequence number already served,
+ * `id` the nonzero value it keeps in state while alive */
+int fgk_launch_static_serve(const fgk_plan *p, int v, fgk_serve_words w, uint64_t seen, uint64_t id,
+                            uint32_t idle_polls, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

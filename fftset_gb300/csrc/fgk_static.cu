@@ -200,6 +200,33 @@ extern "C" int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, s
 	return (int)cudaGetLastError();
 }
 
+extern "C" int fgk_static_serve_ok(uint32_t mod, uint32_t L, int v, int op)
+{
+	const fgk::StaticEntry *e;
+	const int nv = fgk::variants(mod, L, &e);
+	return v >= 0 && v < nv && e[v].serve && op >= 0 && op < FGK_OP_COUNT && ((e[v].serve_ops >> op) & 1u);
+}
+
+extern "C" int fgk_launch_static_serve(const fgk_plan *p, int v, fgk_serve_words w, uint64_t seen, uint64_t id,
+                                       uint32_t idle_polls, void *stream)
+{
+	using namespace fgk;
+	const StaticEntry *e;
+	const int nv = variants(p->modulation, p->L, &e);
+	if (v < 0 || v >= nv || !e[v].serve || id == 0 || idle_polls == 0)
+		return -1;
+	e += v;
+	int per_sm = 0;
+	cudaError_t err = launch_setup((const void *)e->serve, (int)e->T, e->serve_smem, &per_sm);
+	if (err != cudaSuccess)
+		return (int)err;
+	if (per_sm < 1)
+		return (int)cudaErrorInvalidConfiguration;
+	e->serve<<<1, e->T, e->serve_smem, (cudaStream_t)stream>>>(*p, w, seen, id, idle_polls);
+	fgk_count_launch();
+	return (int)cudaGetLastError();
+}
+
 extern "C" int fgk_static_ola_variant(uint32_t mod, uint32_t L)
 {
 	const fgk::StaticEntry *e;

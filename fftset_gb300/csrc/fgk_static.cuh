@@ -1191,12 +1191,138 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_adj(const fgk_pla
 	}
 }
 
+/* ---- call service --------------------------------------------------------
+ * One CTA of one group (T threads) serving single transforms of this
+ * configuration on request (fgk.h, fgk_serve_words): the tables are staged
+ * once, then each request runs the same stages as the batched kernel of the
+ * op (so the same bits), and no request costs a launch. Thread 0 polls the
+ * host-mapped doorbell, at most idle_polls times in a row; the CTA exits
+ * after writing 0 to `state` and finding the doorbell unchanged once more
+ * behind a system-scope fence (the host stores the doorbell and fences
+ * before it reads `state`, so one of the two sees the other). */
+__device__ __forceinline__ uint64_t sv_ld_acquire(const volatile uint64_t *p)
+{
+	uint64_t v;
+	asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ uint64_t sv_ld_relaxed(const volatile void *p)
+{
+	uint64_t v;
+	asm volatile("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ void sv_st_release(volatile uint64_t *p, uint64_t v)
+{
+	asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void sv_st_relaxed(volatile uint64_t *p, uint64_t v)
+{
+	asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <class C, int OP>
+__device__ __forceinline__ void serve_one(int tid, float2 *exb, const float *in, float *out, const float2 *tws,
+                                          const float2 *mods, const float2 *ks)
+{
+	const FirstLoad<C, OP, false> first{in, mods};
+	if constexpr (C::PP)
+		pp_transform<C, OP>(tid, 0, exb, exb + C::SLOTS, first, out, tws, mods, ks);
+	else
+		transform<C, OP, false>(tid, 0, Ex<C>{exb}, first, out, tws, mods, ks);
+}
+
+template <class C, int OPS>
+__global__ void __launch_bounds__(C::T, 1)
+    static_kernel_serve(const fgk_plan p, fgk_serve_words w, uint64_t seen, uint64_t id, uint32_t idle_polls)
+{
+	static_assert(!C::TMA, "the call service runs the direct or ping-pong stages");
+	extern __shared__ float2 smem[];
+	using Lay = Layout<C, FGK_OP_CONV>; /* the tables with room for the kernel spectrum */
+	const float2 *tws = C::TWG ? (const float2 *)p.tw : smem;
+	float2 *mods = smem + Lay::TW;
+	float2 *ks = mods + Lay::MODS;
+	float2 *exb = ks + Lay::KS;
+	__shared__ int s_op;
+	__shared__ uint64_t s_seq, s_in, s_out, s_kern;
+	stage_tables<C, FGK_OP_FORWARD>(p, StaticArgs{}, smem, mods, nullptr);
+	const int tid = C::wt((int)threadIdx.x, 0);
+	for (;;) {
+		if (threadIdx.x == 0) {
+			uint64_t b = sv_ld_acquire(w.bell);
+			for (uint32_t polls = 1; b == seen; polls++) {
+				if (polls >= idle_polls) {
+					sv_st_release(w.state, 0); /* exiting */
+					asm volatile("fence.sc.sys;" ::: "memory");
+					b = sv_ld_acquire(w.bell);
+					if (b != seen)
+						sv_st_relaxed(w.state, id); /* a request came in meanwhile: stay */
+					break;
+				}
+				b = sv_ld_acquire(w.bell);
+			}
+			s_op = -1;
+			if (b != seen) {
+				s_op = (int)(int32_t)(uint32_t)sv_ld_relaxed(&w.req->op);
+				s_in = sv_ld_relaxed(&w.req->in);
+				s_out = sv_ld_relaxed(&w.req->out);
+				s_kern = sv_ld_relaxed(&w.req->kern);
+				s_seq = b;
+				seen = b;
+			}
+		}
+		__syncthreads();
+		const int op = s_op;
+		if (op < 0)
+			break;
+		const float *in = reinterpret_cast<const float *>(s_in);
+		float *out = reinterpret_cast<float *>(s_out);
+		if (op == FGK_OP_CONV || op == FGK_OP_CORR) {
+			/* the request's kernel spectrum, as the batched kernel stages it */
+			const float *kern = reinterpret_cast<const float *>(s_kern);
+			const int32_t *kidx = p.kidx;
+			const int kvw = (int)p.kvw;
+			for (int i = threadIdx.x; i < C::L; i += blockDim.x) {
+				const int o = __ldg(kidx + i);
+				float2 k = make_float2(__ldg(kern + o), __ldg(kern + o + kvw));
+				if (op == FGK_OP_CORR)
+					k.y = -k.y;
+				ks[i] = k;
+			}
+			__syncthreads();
+		}
+		if constexpr ((OPS >> FGK_OP_FORWARD) & 1)
+			if (op == FGK_OP_FORWARD)
+				serve_one<C, FGK_OP_FORWARD>(tid, exb, in, out, tws, mods, ks);
+		if constexpr ((OPS >> FGK_OP_INVERSE) & 1)
+			if (op == FGK_OP_INVERSE)
+				serve_one<C, FGK_OP_INVERSE>(tid, exb, in, out, tws, mods, ks);
+		if constexpr ((OPS >> FGK_OP_CONV) & 1)
+			if (op == FGK_OP_CONV)
+				serve_one<C, FGK_OP_CONV>(tid, exb, in, out, tws, mods, ks);
+		if constexpr ((OPS >> FGK_OP_CORR) & 1)
+			if (op == FGK_OP_CORR)
+				serve_one<C, FGK_OP_CORR>(tid, exb, in, out, tws, mods, ks);
+		/* every thread's stores, then one system-scope release of the
+		 * sequence number (cumulative over the CTA's stores) */
+		__syncthreads();
+		if (threadIdx.x == 0)
+			sv_st_release(w.reply, s_seq);
+	}
+}
+
+template <class C> constexpr size_t serve_smem_bytes()
+{
+	return sizeof(float2) * (Layout<C, FGK_OP_CONV>::TABLES + (C::PP ? 2 : 1) * (size_t)C::SLOTS);
+}
+
 /* ------------------------------------------------------------------------
  * Registry entries */
 typedef void (*static_fn)(const fgk_plan, StaticArgs);
 typedef void (*kgrad_fn)(const fgk_plan, KgradArgs);
 typedef void (*adj_fn)(const fgk_plan, AdjArgs);
 typedef void (*ola_fn)(const fgk_plan, OlaArgs);
+typedef void (*serve_fn)(const fgk_plan, fgk_serve_words, uint64_t, uint64_t, uint32_t);
 
 struct StaticEntry {
 	uint32_t  mod, L, T, G, n, tma;
@@ -1209,6 +1335,9 @@ struct StaticEntry {
 	size_t    adj_smem;
 	ola_fn    ola; /* the fused overlap-add, or null */
 	size_t    ola_smem;
+	serve_fn  serve; /* the call service, or null */
+	size_t    serve_smem;
+	uint32_t  serve_ops;
 };
 
 template <class C, int OP> constexpr size_t smem_bytes()
@@ -1285,6 +1414,17 @@ template <class C> StaticEntry with_ola(StaticEntry e)
 	static_assert(smem_bytes<C, FGK_OP_CONV>() <= FGK_SMEM_LIMIT, "overlap-add kernel exceeds shared memory");
 	e.ola = static_kernel_ola<C>;
 	e.ola_smem = smem_bytes<C, FGK_OP_CONV>();
+	return e;
+}
+
+/* adds the call service to an entry (configurations without bulk-copy
+ * input), for the ops the entry compiles */
+template <class C, int OPS> StaticEntry with_serve(StaticEntry e)
+{
+	static_assert(serve_smem_bytes<C>() <= FGK_SMEM_LIMIT, "call service exceeds shared memory");
+	e.serve = static_kernel_serve<C, OPS>;
+	e.serve_smem = serve_smem_bytes<C>();
+	e.serve_ops = (uint32_t)OPS;
 	return e;
 }
 

@@ -16,7 +16,7 @@ int static_entries_1024(const StaticEntry **out)
 	static StaticEntry t[3];
 	static bool init = false;
 	if (!init) {
-		t[0] = make_entry<V0, OPS_ALL>();
+		t[0] = with_serve<V0, OPS_ALL>(make_entry<V0, OPS_ALL>());
 		t[1] = make_entry<V1, OPS_ALL>();
 		t[2] = make_entry<V2, OPS_ALL>();
 		init = true;

@@ -59,7 +59,7 @@ int static_entries_1536(const StaticEntry **out)
 	static StaticEntry t[14];
 	static bool init = false;
 	if (!init) {
-		t[0] = with_ola<V0>(make_entry<V0, OPS_ALL>());
+		t[0] = with_serve<V0, OPS_ALL>(with_ola<V0>(make_entry<V0, OPS_ALL>()));
 		t[1] = make_entry<V1, OPS_CONV_CORR>();
 		t[2] = make_entry<V2, OPS_CONV_CORR>();
 		t[3] = make_entry<V3, OPS_CONV_CORR>();

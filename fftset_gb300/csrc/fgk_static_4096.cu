@@ -38,8 +38,8 @@ int static_entries_4096(const StaticEntry **out)
 	static StaticEntry t[10];
 	static bool init = false;
 	if (!init) {
-		t[0] = make_entry<V7, 1 << FGK_OP_INVERSE>();
-		t[1] = with_kgrad<V0>(make_entry<V0, OPS_ALL>());
+		t[0] = with_serve<V7, 1 << FGK_OP_INVERSE>(make_entry<V7, 1 << FGK_OP_INVERSE>());
+		t[1] = with_serve<V0, OPS_ALL>(with_kgrad<V0>(make_entry<V0, OPS_ALL>()));
 		t[2] = make_entry<V1, OPS_ALL>();
 		t[3] = make_entry<V2, OPS_CONV_CORR>();
 		t[4] = make_entry<V3, OPS_CONV_CORR>();

@@ -24,7 +24,7 @@ int static_entries_c1536(const StaticEntry **out)
 	static StaticEntry t[2];
 	static bool init = false;
 	if (!init) {
-		t[0] = make_entry<C1536a, OPS_ALL>();
+		t[0] = with_serve<C1536a, OPS_ALL>(make_entry<C1536a, OPS_ALL>());
 		t[1] = make_entry<C1536b, OPS_ALL>();
 		init = true;
 	}
@@ -37,7 +37,7 @@ int static_entries_c4096(const StaticEntry **out)
 	static StaticEntry t[2];
 	static bool init = false;
 	if (!init) {
-		t[0] = make_entry<C4096a, OPS_ALL>();
+		t[0] = with_serve<C4096a, OPS_ALL>(make_entry<C4096a, OPS_ALL>());
 		t[1] = make_entry<C4096b, OPS_ALL>();
 		init = true;
 	}
