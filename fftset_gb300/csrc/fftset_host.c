@@ -867,9 +867,10 @@ static int fs_exec_pipelined(const struct fftset_fft *f, int op, float *out, siz
 }
 
 /* ---- the call service ----------------------------------------------------
- * Blocking single calls on device buffers of a compiled variant that has a
- * call service (fgk.h) are answered by one resident CTA instead of a launch
- * and a stream synchronisation: the request goes into a pinned, mapped page,
+ * Blocking single calls on device buffers of resident sizes (the op's
+ * compiled variant when it has a call service, else the generic kernel's,
+ * fgk.h) are answered by one resident CTA instead of a launch and a stream
+ * synchronisation: the request goes into a pinned, mapped page,
  * the doorbell is a sequence number, and the call returns when the CTA has
  * published that number in `reply` (its output stores released before it).
  * A launch of the service is made only when the same (plan, variant) is
@@ -914,7 +915,8 @@ static int fs_serve_launch(struct fs_impl *fs, const struct fftset_fft *f, int v
 	const uint64_t id = ++s->id;
 	int rc;
 	__atomic_store_n(s->state, id, __ATOMIC_RELEASE);
-	rc = fgk_launch_static_serve(&f->vp[v], v, s->dev, seen, id, s->idle_polls, s->stream);
+	rc = v < 0 ? fgk_launch_resident_serve(&f->rp, s->dev, seen, id, s->idle_polls, s->stream)
+	           : fgk_launch_static_serve(&f->vp[v], v, s->dev, seen, id, s->idle_polls, s->stream);
 	if (rc != 0) {
 		cudaGetLastError();
 		__atomic_store_n(s->state, 0, __ATOMIC_RELEASE);
@@ -950,7 +952,10 @@ static int fs_serve_call(const struct fftset_fft *f, int v, int op, float *out, 
 	unsigned relaunch = 0;
 	uint32_t polls;
 	cudaError_t e;
-	if (!s->idle_polls || s->broken || !fgk_static_serve_ok(f->rp.modulation, f->lfft, v, op))
+	if (!s->idle_polls || s->broken || f->fourstep || op < 0 || op >= FGK_OP_COUNT)
+		return -1;
+	/* v < 0: the generic kernel, whose service takes every op */
+	if (v >= 0 && !fgk_static_serve_ok(f->rp.modulation, f->lfft, v, op))
 		return -1;
 	pthread_mutex_lock(&fs->lock);
 	if (s->last_f != f || s->last_v != v) {

@@ -291,6 +291,10 @@ int fgk_static_serve_ok(uint32_t modulation, uint32_t L, int v, int op);
  * `id` the nonzero value it keeps in state while alive */
 int fgk_launch_static_serve(const fgk_plan *p, int v, fgk_serve_words w, uint64_t seen, uint64_t id,
                             uint32_t idle_polls, void *stream);
+/* the same for the generic resident kernel (any resident plan, every op,
+ * the results of fgk_launch_resident bit for bit) */
+int fgk_launch_resident_serve(const fgk_plan *p, fgk_serve_words w, uint64_t seen, uint64_t id, uint32_t idle_polls,
+                              void *stream);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,7 @@
 #include <stdint.h>
 #include "fgk.h"
 #include "fgk_codelets.cuh"
+#include "fgk_serve.cuh"
 
 namespace fgk {
 
@@ -148,24 +149,14 @@ __device__ __forceinline__ void fused_sm(const Group &g, const fgk_stage &stf, c
 	__syncthreads();
 }
 
-/* Generic resident kernel: any plan, any op. The modulation edges run as a
- * prologue (HBM -> shared memory) and an epilogue (shared memory -> HBM);
- * the chain between them is shared by all ops. */
+/* One transform by one group (every thread of the CTA calls it: the stages
+ * end in CTA barriers): x the block's input, y its output. The modulation
+ * edges run as a prologue (HBM -> shared memory) and an epilogue (shared
+ * memory -> HBM); the chain between them is shared by all ops. */
 template <int EMAX>
-__global__ void __launch_bounds__(1024, 1) resident_generic(const fgk_plan p, int op, float *out, const float *in,
-                                                         const float *__restrict__ kern, uint32_t count,
-                                                         size_t in_stride, size_t out_stride)
+__device__ __forceinline__ void generic_one(const fgk_plan &p, Group &g, int op, float *y, const float *x,
+                                            const float *__restrict__ kern)
 {
-	extern __shared__ float2 smem[];
-	Group g;
-	g.L = (int)p.L;
-	g.T = (int)p.threads;
-	g.pad = (int)p.pad;
-	const int grp = (int)(threadIdx.x / p.threads);
-	g.ltid = (int)threadIdx.x - grp * g.T;
-	const uint64_t t = (uint64_t)blockIdx.x * p.per_cta + (uint64_t)grp;
-	g.active = grp < (int)p.per_cta && t < count;
-	g.sm = smem + (size_t)(grp < (int)p.per_cta ? grp : 0) * p.smem_stride;
 	const int L = g.L;
 	const bool freqoff = p.modulation == FGK_MOD_FREQOFF;
 	const float2 *tw = (const float2 *)p.tw;
@@ -175,7 +166,6 @@ __global__ void __launch_bounds__(1024, 1) resident_generic(const fgk_plan p, in
 
 	/* prologue: the sequence to transform, natural order, into shared memory */
 	if (g.active) {
-		const float *x = in + t * in_stride;
 		if (!inverse) {
 			if (freqoff) {
 				for (int i = g.ltid; i < L; i += g.T)
@@ -226,7 +216,6 @@ __global__ void __launch_bounds__(1024, 1) resident_generic(const fgk_plan p, in
 	/* epilogue */
 	if (!g.active)
 		return;
-	float *y = out + t * out_stride;
 	if (inverse || conv) {
 		/* u = DFT(conj(.)): FREQ_OFFSET_REAL y[i] + j y[L+i] = u_i e^{-j pi i/(2L)};
 		 * COMPLEX y = conj(u) */
@@ -267,7 +256,59 @@ __global__ void __launch_bounds__(1024, 1) resident_generic(const fgk_plan p, in
 	}
 }
 
+/* Generic resident kernel: any plan, any op, per_cta groups per CTA. */
+template <int EMAX>
+__global__ void __launch_bounds__(1024, 1) resident_generic(const fgk_plan p, int op, float *out, const float *in,
+                                                         const float *__restrict__ kern, uint32_t count,
+                                                         size_t in_stride, size_t out_stride)
+{
+	extern __shared__ float2 smem[];
+	Group g;
+	g.L = (int)p.L;
+	g.T = (int)p.threads;
+	g.pad = (int)p.pad;
+	const int grp = (int)(threadIdx.x / p.threads);
+	g.ltid = (int)threadIdx.x - grp * g.T;
+	const uint64_t t = (uint64_t)blockIdx.x * p.per_cta + (uint64_t)grp;
+	g.active = grp < (int)p.per_cta && t < count;
+	g.sm = smem + (size_t)(grp < (int)p.per_cta ? grp : 0) * p.smem_stride;
+	const uint64_t tt = g.active ? t : 0;
+	generic_one<EMAX>(p, g, op, out + tt * out_stride, in + tt * in_stride, kern);
+}
+
+/* The call service of the generic kernel (fgk.h, fgk_serve_words; the
+ * doorbell protocol is fgk_serve.cuh's): one CTA, one group, one transform
+ * per request through the same stages as resident_generic, so the same
+ * bits, without a launch per request. */
+template <int EMAX>
+__global__ void __launch_bounds__(1024, 1) resident_serve(const fgk_plan p, fgk_serve_words w, uint64_t seen,
+                                                       uint64_t id, uint32_t idle_polls)
+{
+	extern __shared__ float2 smem[];
+	__shared__ ServeSlot slot;
+	Group g;
+	g.L = (int)p.L;
+	g.T = (int)p.threads;
+	g.pad = (int)p.pad;
+	g.ltid = (int)threadIdx.x;
+	g.active = (int)threadIdx.x < g.T;
+	g.sm = smem;
+	for (;;) {
+		if (threadIdx.x == 0)
+			serve_next(w, seen, id, idle_polls, slot);
+		__syncthreads();
+		if (slot.op < 0)
+			break;
+		generic_one<EMAX>(p, g, slot.op, reinterpret_cast<float *>(slot.out),
+		                  reinterpret_cast<const float *>(slot.in), reinterpret_cast<const float *>(slot.kern));
+		__syncthreads();
+		if (threadIdx.x == 0)
+			serve_reply(w, slot);
+	}
+}
+
 typedef void (*resident_fn)(const fgk_plan, int, float *, const float *, const float *, uint32_t, size_t, size_t);
+typedef void (*resident_serve_fn)(const fgk_plan, fgk_serve_words, uint64_t, uint64_t, uint32_t);
 
 } /* namespace fgk */
 
@@ -281,6 +322,25 @@ extern "C" void fgk_count_launch(void)
 extern "C" unsigned long long fftset__launch_count(void)
 {
 	return __atomic_load_n(&fgk_launches, __ATOMIC_RELAXED);
+}
+
+extern "C" int fgk_launch_resident_serve(const fgk_plan *p, fgk_serve_words w, uint64_t seen, uint64_t id,
+                                         uint32_t idle_polls, void *stream)
+{
+	using namespace fgk;
+	if (id == 0 || idle_polls == 0 || p->threads == 0 || p->threads > 1024)
+		return -1;
+	resident_serve_fn fn = p->emax > 16 ? resident_serve<32> : resident_serve<16>;
+	const uint32_t threads = (p->threads + 31u) & ~31u;
+	const size_t smem = (size_t)p->smem_stride * sizeof(float2);
+	if (smem > 48 * 1024) {
+		cudaError_t e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess)
+			return (int)e;
+	}
+	fn<<<1, threads, smem, (cudaStream_t)stream>>>(*p, w, seen, id, idle_polls);
+	fgk_count_launch();
+	return (int)cudaGetLastError();
 }
 
 extern "C" uint32_t fgk_max_resident_L(void)

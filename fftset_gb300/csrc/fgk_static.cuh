@@ -23,6 +23,7 @@
 #include <stdint.h>
 #include "fgk.h"
 #include "fgk_codelets.cuh"
+#include "fgk_serve.cuh"
 
 namespace fgk {
 
@@ -1193,34 +1194,10 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_adj(const fgk_pla
 
 /* ---- call service --------------------------------------------------------
  * One CTA of one group (T threads) serving single transforms of this
- * configuration on request (fgk.h, fgk_serve_words): the tables are staged
- * once, then each request runs the same stages as the batched kernel of the
- * op (so the same bits), and no request costs a launch. Thread 0 polls the
- * host-mapped doorbell, at most idle_polls times in a row; the CTA exits
- * after writing 0 to `state` and finding the doorbell unchanged once more
- * behind a system-scope fence (the host stores the doorbell and fences
- * before it reads `state`, so one of the two sees the other). */
-__device__ __forceinline__ uint64_t sv_ld_acquire(const volatile uint64_t *p)
-{
-	uint64_t v;
-	asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-	return v;
-}
-__device__ __forceinline__ uint64_t sv_ld_relaxed(const volatile void *p)
-{
-	uint64_t v;
-	asm volatile("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-	return v;
-}
-__device__ __forceinline__ void sv_st_release(volatile uint64_t *p, uint64_t v)
-{
-	asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ void sv_st_relaxed(volatile uint64_t *p, uint64_t v)
-{
-	asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
+ * configuration on request (fgk.h, fgk_serve_words; the doorbell protocol
+ * is fgk_serve.cuh's): the tables are staged once, then each request runs
+ * the same stages as the batched kernel of the op (so the same bits), and
+ * no request costs a launch. */
 template <class C, int OP>
 __device__ __forceinline__ void serve_one(int tid, float2 *exb, const float *in, float *out, const float2 *tws,
                                           const float2 *mods, const float2 *ks)
@@ -1243,43 +1220,21 @@ __global__ void __launch_bounds__(C::T, 1)
 	float2 *mods = smem + Lay::TW;
 	float2 *ks = mods + Lay::MODS;
 	float2 *exb = ks + Lay::KS;
-	__shared__ int s_op;
-	__shared__ uint64_t s_seq, s_in, s_out, s_kern;
+	__shared__ ServeSlot slot;
 	stage_tables<C, FGK_OP_FORWARD>(p, StaticArgs{}, smem, mods, nullptr);
 	const int tid = C::wt((int)threadIdx.x, 0);
 	for (;;) {
-		if (threadIdx.x == 0) {
-			uint64_t b = sv_ld_acquire(w.bell);
-			for (uint32_t polls = 1; b == seen; polls++) {
-				if (polls >= idle_polls) {
-					sv_st_release(w.state, 0); /* exiting */
-					asm volatile("fence.sc.sys;" ::: "memory");
-					b = sv_ld_acquire(w.bell);
-					if (b != seen)
-						sv_st_relaxed(w.state, id); /* a request came in meanwhile: stay */
-					break;
-				}
-				b = sv_ld_acquire(w.bell);
-			}
-			s_op = -1;
-			if (b != seen) {
-				s_op = (int)(int32_t)(uint32_t)sv_ld_relaxed(&w.req->op);
-				s_in = sv_ld_relaxed(&w.req->in);
-				s_out = sv_ld_relaxed(&w.req->out);
-				s_kern = sv_ld_relaxed(&w.req->kern);
-				s_seq = b;
-				seen = b;
-			}
-		}
+		if (threadIdx.x == 0)
+			serve_next(w, seen, id, idle_polls, slot);
 		__syncthreads();
-		const int op = s_op;
+		const int op = slot.op;
 		if (op < 0)
 			break;
-		const float *in = reinterpret_cast<const float *>(s_in);
-		float *out = reinterpret_cast<float *>(s_out);
+		const float *in = reinterpret_cast<const float *>(slot.in);
+		float *out = reinterpret_cast<float *>(slot.out);
 		if (op == FGK_OP_CONV || op == FGK_OP_CORR) {
 			/* the request's kernel spectrum, as the batched kernel stages it */
-			const float *kern = reinterpret_cast<const float *>(s_kern);
+			const float *kern = reinterpret_cast<const float *>(slot.kern);
 			const int32_t *kidx = p.kidx;
 			const int kvw = (int)p.kvw;
 			for (int i = threadIdx.x; i < C::L; i += blockDim.x) {
@@ -1303,11 +1258,9 @@ __global__ void __launch_bounds__(C::T, 1)
 		if constexpr ((OPS >> FGK_OP_CORR) & 1)
 			if (op == FGK_OP_CORR)
 				serve_one<C, FGK_OP_CORR>(tid, exb, in, out, tws, mods, ks);
-		/* every thread's stores, then one system-scope release of the
-		 * sequence number (cumulative over the CTA's stores) */
 		__syncthreads();
 		if (threadIdx.x == 0)
-			sv_st_release(w.reply, s_seq);
+			serve_reply(w, slot);
 	}
 }
 

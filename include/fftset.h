@@ -120,10 +120,9 @@ void *fftset_get_stream(const struct fftset *fc);
 void *fftset_own_stream(const struct fftset *fc);
 /* 1 (default): calls return after their results are in place. 0: calls
  * with device buffers only enqueue work on the stream.
- * Blocking single calls (forward, inverse, conv, their correlation form)
- * on device buffers of a size with compiled kernels are answered, from the
- * second such call in a row, by a resident one-CTA service on a stream of
- * its own: the call waits for the work queued on the fftset's stream,
+ * Blocking single calls on device buffers of sizes up to the shared-memory
+ * limit are answered, from the second such call of the same size and kernel
+ * in a row, by a resident one-CTA service on a stream of its own: the call waits for the work queued on the fftset's stream,
  * hands the request over through host-mapped memory and returns when the
  * results are in place, with the same bits as the batched kernels and no
  * launch of its own. The service exits after about 50 us without requests

@@ -1,9 +1,9 @@
-"""The call service: blocking single calls on device buffers of a compiled
-size are answered by one resident CTA instead of a launch each. Its results
-must be the batched kernels' bit for bit, it must wait for work already
-queued on the fftset's stream, and it must come and go (idle exit, a new
-launch on the next call, destroy while it is live) without changing a
-result."""
+"""The call service: blocking single calls on device buffers of resident
+sizes are answered by one resident CTA (the compiled variant's service, or
+the generic kernel's) instead of a launch each. Its results must be the
+batched kernels' bit for bit, it must wait for work already queued on the
+fftset's stream, and it must come and go (idle exit, a new launch on the
+next call, destroy while it is live) without changing a result."""
 import ctypes as C
 import time
 
@@ -24,7 +24,8 @@ def _hooks(lib):
     return L
 
 
-@pytest.mark.parametrize("mod,L", [(0, 1024), (1, 1536), (1, 4096)])
+@pytest.mark.parametrize("mod,L", [(0, 1024), (1, 1536), (1, 4096),  # compiled kernels' services
+                                   (0, 2048), (1, 45), (0, 27), (1, 19683)])  # the generic kernel's
 def test_served_calls_equal_batched_kernels(fftset_lib, mod, L):
     import torch
     H = _hooks(fftset_lib)
@@ -37,8 +38,9 @@ def test_served_calls_equal_batched_kernels(fftset_lib, mod, L):
         h = rng.standard_normal(2 * L).astype(np.float32)
         K = torch.empty(2 * L, device="cuda")
         f.conv_get_kernel(K, torch.from_numpy(h).cuda())
+        ops = ("forward", "inverse", "conv", "conv_get_kernel")
         want = {}
-        for op in ("forward", "inverse", "conv"):
+        for op in ops:
             y = torch.empty_like(x)
             if op == "conv":
                 f.conv_batch(y, x, K)
@@ -46,7 +48,7 @@ def test_served_calls_equal_batched_kernels(fftset_lib, mod, L):
                 getattr(f, op + "_batch")(y, x)
             want[op] = y.cpu().numpy()
         n0 = H.fftset__test_served_calls(S.handle)
-        for op in ("forward", "inverse", "conv"):
+        for op in ops:
             got = torch.full_like(x, 7.0)
             for b in range(B):  # repeated calls of one kind: the service takes them
                 if op == "conv":
