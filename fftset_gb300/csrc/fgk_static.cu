@@ -123,9 +123,23 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 	if (grid > need)
 		grid = need;
 	StaticArgs a{out, in, kern, count, in_stride, out_stride, err_flag};
-	e->fn[op]<<<(unsigned)grid, e->T * e->G, smem, (cudaStream_t)stream>>>(*p, a);
+	/* programmatic stream serialisation: the kernel waits for the launches
+	 * before it (griddepcontrol.wait in stage_tables) before it reads what
+	 * they may have written */
+	cudaLaunchConfig_t cfg = {};
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.gridDim = dim3((unsigned)grid);
+	cfg.blockDim = dim3(e->T * e->G);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = (cudaStream_t)stream;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	const fgk_plan pc = *p;
+	const cudaError_t le = cudaLaunchKernelEx(&cfg, e->fn[op], pc, a);
 	fgk_count_launch();
-	return (int)cudaGetLastError();
+	return le != cudaSuccess ? (int)le : (int)cudaGetLastError();
 }
 
 extern "C" int fgk_static_kgrad_variant(uint32_t mod, uint32_t L)

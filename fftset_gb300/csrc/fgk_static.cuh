@@ -425,12 +425,22 @@ __device__ __forceinline__ void transform(int tid, int g, const Ex<C> &ex, const
 	gsync<C>(g); /* the exchange buffer is reused by the next transform */
 }
 
-/* ---- per-CTA tables ----------------------------------------------------- */
+/* ---- per-CTA tables -----------------------------------------------------
+ * The batched kernels are launched with programmatic stream serialisation
+ * (fgk_launch_static): a CTA lets the next launch on the stream be
+ * scheduled as soon as it starts, stages the plan's twiddles and
+ * modulation factors (written when the plan was made, never by a kernel),
+ * then waits for the launches before it on the stream to finish
+ * (griddepcontrol.wait, which returns at once when there are none) before
+ * it reads anything a kernel may have written: the kernel buffer here, the
+ * input blocks after. The next step's launch and table staging overlap the
+ * tail of this one. */
 template <class C, int OP>
 __device__ __forceinline__ void stage_tables(const fgk_plan &p, const StaticArgs &a, float2 *smem, float2 *mods,
                                              float2 *ks)
 {
 	constexpr int L = C::L;
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 	if constexpr (!C::TWG)
 		stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
 	if constexpr (C::MOD == FGK_MOD_FREQOFF) {
@@ -438,6 +448,7 @@ __device__ __forceinline__ void stage_tables(const fgk_plan &p, const StaticArgs
 		for (int i = threadIdx.x; i < C::NMODS; i += blockDim.x)
 			mods[i] = __ldg(gm + i);
 	}
+	asm volatile("griddepcontrol.wait;" ::: "memory");
 	if constexpr (OP == FGK_OP_CONV || OP == FGK_OP_CORR) {
 		const int32_t *kidx = p.kidx;
 		const int kvw = (int)p.kvw;
