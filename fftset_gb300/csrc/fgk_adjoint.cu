@@ -44,12 +44,17 @@ __global__ void kg_spec_partial(const float2 *__restrict__ S, const float2 *__re
  * FREQ_OFFSET_REAL forward layout from packed-sequence bins (pack == 1).
  * A CTA covers KG_BINS bins with KG_SPLIT threads per bin, each summing every
  * KG_SPLIT-th partial (a warp reads 128-byte runs of two rows), then the
- * KG_SPLIT sums of a bin are added in shared memory in a fixed order. */
+ * KG_SPLIT sums of a bin are added in shared memory in a fixed order.
+ * Launched as a programmatic dependent of the kernel that wrote the
+ * partials (it waits for it before the first read) and lets the inverse
+ * transform after it be scheduled as it starts. */
 constexpr int KG_BINS = 16, KG_SPLIT = 32;
 __global__ void __launch_bounds__(KG_BINS *KG_SPLIT) kg_reduce(const float2 *__restrict__ partials, uint32_t P,
                                                               uint32_t L, int pack, float2 *out)
 {
 	__shared__ float2 part[KG_SPLIT][KG_BINS];
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+	asm volatile("griddepcontrol.wait;" ::: "memory");
 	const uint32_t lane = threadIdx.x % KG_BINS, r0 = threadIdx.x / KG_BINS;
 	const uint32_t i = blockIdx.x * KG_BINS + lane;
 	float2 a = make_float2(0.f, 0.f);
@@ -92,8 +97,17 @@ extern "C" int fgk_launch_kgrad_reduce(const float *partials, uint32_t P, uint32
                                        void *stream)
 {
 	using namespace fgk;
-	kg_reduce<<<(L + KG_BINS - 1) / KG_BINS, KG_BINS * KG_SPLIT, 0, (cudaStream_t)stream>>>(
-	    reinterpret_cast<const float2 *>(partials), P, L, pack, reinterpret_cast<float2 *>(out));
+	cudaLaunchConfig_t cfg = {};
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.gridDim = dim3((L + KG_BINS - 1) / KG_BINS);
+	cfg.blockDim = dim3(KG_BINS * KG_SPLIT);
+	cfg.stream = (cudaStream_t)stream;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	const cudaError_t le = cudaLaunchKernelEx(&cfg, kg_reduce, reinterpret_cast<const float2 *>(partials), P, L, pack,
+	                                          reinterpret_cast<float2 *>(out));
 	fgk_count_launch();
-	return (int)cudaGetLastError();
+	return le != cudaSuccess ? (int)le : (int)cudaGetLastError();
 }

@@ -94,6 +94,25 @@ static cudaError_t launch_setup(const void *fn, int threads, size_t smem, int *p
 	pthread_mutex_unlock(&setup_lock);
 	return e;
 }
+/* a launch with programmatic stream serialisation: the kernel executes
+ * griddepcontrol.wait before it reads what earlier launches may have written
+ * (stage_tables, static_kernel_adj) */
+template <class... Args>
+static cudaError_t launch_dependent(void (*fn)(Args...), unsigned grid, unsigned block, size_t smem,
+                                    cudaStream_t stream, Args... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(block);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, fn, args...);
+}
 } /* namespace fgk */
 
 extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, const float *in, const float *kern,
@@ -123,21 +142,8 @@ extern "C" int fgk_launch_static(const fgk_plan *p, int v, int op, float *out, c
 	if (grid > need)
 		grid = need;
 	StaticArgs a{out, in, kern, count, in_stride, out_stride, err_flag};
-	/* programmatic stream serialisation: the kernel waits for the launches
-	 * before it (griddepcontrol.wait in stage_tables) before it reads what
-	 * they may have written */
-	cudaLaunchConfig_t cfg = {};
-	cudaLaunchAttribute at[1];
-	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-	at[0].val.programmaticStreamSerializationAllowed = 1;
-	cfg.gridDim = dim3((unsigned)grid);
-	cfg.blockDim = dim3(e->T * e->G);
-	cfg.dynamicSmemBytes = smem;
-	cfg.stream = (cudaStream_t)stream;
-	cfg.attrs = at;
-	cfg.numAttrs = 1;
-	const fgk_plan pc = *p;
-	const cudaError_t le = cudaLaunchKernelEx(&cfg, e->fn[op], pc, a);
+	const cudaError_t le =
+	    launch_dependent(e->fn[op], (unsigned)grid, e->T * e->G, smem, (cudaStream_t)stream, *p, a);
 	fgk_count_launch();
 	return le != cudaSuccess ? (int)le : (int)cudaGetLastError();
 }
@@ -177,8 +183,11 @@ extern "C" int fgk_launch_static_kgrad(const fgk_plan *p, int v, const float *g,
 	if (grid == 0)
 		return (int)cudaErrorInvalidValue;
 	KgradArgs a{g, x, g_stride, x_stride, count, reinterpret_cast<float2 *>(partials)};
-	e->kgrad<<<(unsigned)grid, e->T * e->G, e->kgrad_smem, (cudaStream_t)stream>>>(*p, a);
+	const cudaError_t le =
+	    launch_dependent(e->kgrad, (unsigned)grid, e->T * e->G, e->kgrad_smem, (cudaStream_t)stream, *p, a);
 	fgk_count_launch();
+	if (le != cudaSuccess)
+		return (int)le;
 	*rows = (uint32_t)grid;
 	return (int)cudaGetLastError();
 }
@@ -208,8 +217,11 @@ extern "C" int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, s
 	if (grid == 0)
 		return (int)cudaErrorInvalidValue;
 	AdjArgs a{g, x, kern, dx, g_stride, x_stride, dx_stride, count, reinterpret_cast<float2 *>(partials)};
-	e->adj<<<(unsigned)grid, e->T * e->G, e->adj_smem, (cudaStream_t)stream>>>(*p, a);
+	const cudaError_t le =
+	    launch_dependent(e->adj, (unsigned)grid, e->T * e->G, e->adj_smem, (cudaStream_t)stream, *p, a);
 	fgk_count_launch();
+	if (le != cudaSuccess)
+		return (int)le;
 	*rows = (uint32_t)grid;
 	return (int)cudaGetLastError();
 }

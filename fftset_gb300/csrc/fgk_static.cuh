@@ -1096,11 +1096,15 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_adj(const fgk_pla
 	float2 *ks = mods + Lay::MODS;
 	float2 *exb = ks + L;
 	float2 *park = exb + (size_t)C::G * C::SLOTS;
+	/* a programmatic dependent, as stage_tables describes: the plan's
+	 * tables before the wait, the kernel buffer and the blocks after */
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 	if constexpr (!C::TWG)
 		stage_twiddles<C, 1>(smem, (const float2 *)p.tw);
 	if constexpr (FREQ)
 		for (int i = threadIdx.x; i < Lay::MODS; i += blockDim.x)
 			mods[i] = __ldg((const float2 *)p.modtw + i);
+	asm volatile("griddepcontrol.wait;" ::: "memory");
 	for (int i = threadIdx.x; i < L; i += blockDim.x) {
 		const int o = __ldg(p.kidx + i);
 		ks[i] = make_float2(__ldg(a.kern + o), -__ldg(a.kern + o + (int)p.kvw)); /* conj K: correlation */
