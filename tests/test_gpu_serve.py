@@ -141,3 +141,47 @@ def test_destroy_with_live_service(fftset_lib):
         S.close()
         assert time.perf_counter() - t0 < 1.0
         torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("mod,L", [(1, 1536), (1, 4096), (0, 1024)])
+def test_dependent_launch_chain(fftset_lib, mod, L):
+    """The compiled kernels, the adjoint kernels and the taps reduction are
+    launched as programmatic dependents: each reads what the launches before
+    it wrote only after griddepcontrol.wait. A chain of non-blocking calls
+    that each consume the previous one's output, with no synchronisation in
+    between, must give the FP64 results."""
+    import torch
+    S = fftset_lib.FftSet()
+    try:
+        f = S.create_fft(mod, L)
+        rng = np.random.default_rng(L + 3)
+        B = 64
+        x_np = rng.standard_normal((B, 2 * L)).astype(np.float32)
+        h_np = rng.standard_normal((B, 2 * L)).astype(np.float32)
+        g_np = rng.standard_normal((B, 2 * L)).astype(np.float32)
+        x, h, g = (torch.from_numpy(a).cuda() for a in (x_np, h_np, g_np))
+        K = torch.empty_like(h)
+        y = torch.empty_like(x)
+        X = torch.empty_like(x)
+        r = torch.empty_like(x)
+        dx = torch.empty_like(x)
+        dh = torch.empty(2 * L, device="cuda")
+        torch.cuda.synchronize()
+        S.set_blocking(False)
+        for _ in range(3):
+            f.conv_get_kernel_batch(K, h)       # K written ...
+            f.conv_batch(y, x, K[0])            # ... read by the next launch
+            f.forward_batch(X, y)               # y read
+            f.inverse_batch(r, X)               # X read
+            f.conv_adjoint_batch(dx, dh, r, x, K[0])  # r, K read; kgrad, reduce, inverse
+        torch.cuda.synchronize()
+        S.set_blocking(True)
+        S.check()
+        y64 = O.conv64(mod, x_np, h_np[0])
+        assert O.rel_l2(y.cpu().numpy(), y64) <= O.tolerance(2 * L if mod else L)
+        assert O.rel_l2(r.cpu().numpy() / L, y64) <= 2 * O.tolerance(2 * L if mod else L)
+        wx, wh = O.conv_adjoint64(mod, x_np, h_np[0], r.cpu().numpy().astype(np.float64))
+        assert O.rel_l2(dx.cpu().numpy(), wx) <= 4 * O.tolerance(2 * L if mod else L)
+        assert O.rel_l2(dh.cpu().numpy(), wh) <= 4 * O.tolerance(2 * L if mod else L)
+    finally:
+        S.close()
