@@ -54,14 +54,24 @@ int fftset_fft_conv_overlap_add(const struct fftset_fft *fft, float *output_buf,
 	if (!cplx && B + kernel_length - 1 <= 2 * B &&
 	    (input_buf + samples <= output_buf || output_buf + samples + kernel_length - 1 <= input_buf)) {
 		/* the compiled fused form where the size has it: the blocks are read
-		 * from the signal and their results added into the output, with at
-		 * most two additions per output sample (the output is zeroed first,
-		 * so it must not overlap the signal) */
+		 * from the signal and their results written into the output, added
+		 * where two blocks meet (at most two additions per output sample;
+		 * those overlap zones, the first K - 1 samples of every B, are
+		 * zeroed first, so the output must not overlap the signal) */
 		const int v = fgk_static_ola_variant(FGK_MOD_FREQOFF, fft->lfft);
 		if (v >= 0 && v < fft->nvar) {
-			if ((rc = fs_cuda(fs, cudaMemsetAsync(output_buf, 0, (samples + kernel_length - 1) * sizeof(float),
-			                                      fs->stream))) != 0)
-				goto done;
+			const size_t nout = samples + kernel_length - 1, ovl = kernel_length - 1;
+			if (ovl) {
+				/* rows of ovl floats, B apart; the last segment start may
+				 * leave fewer than ovl samples before the end */
+				const size_t full = nout >= ovl ? (nout - ovl) / B + 1 : 0, last = full * B;
+				if (full && (rc = fs_cuda(fs, cudaMemset2DAsync(output_buf, B * sizeof(float), 0, ovl * sizeof(float),
+				                                               full, fs->stream))) != 0)
+					goto done;
+				if (last < nout && (rc = fs_cuda(fs, cudaMemsetAsync(output_buf + last, 0,
+				                                                     (nout - last) * sizeof(float), fs->stream))) != 0)
+					goto done;
+			}
 			rc = fgk_launch_static_ola(&fft->vp[v], v, input_buf, samples, (uint32_t)B,
 			                           (uint32_t)(B + kernel_length - 1), (uint32_t)nblocks,
 			                           samples + kernel_length - 1, kernel_buf, output_buf, fs->stream, fs->num_sms);

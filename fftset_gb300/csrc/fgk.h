@@ -250,8 +250,9 @@ int fgk_launch_static_adj(const fgk_plan *p, int v, const float *g, size_t g_str
 
 /* The fused overlap-add (static_kernel_ola): the first compiled variant of
  * (modulation, L) that has it, or -1; the launch convolves the nblocks
- * zero-padded blocks of B samples of `in` and adds the first span samples
- * of each result into `out` (zeroed by the caller) at b B. The caller
+ * zero-padded blocks of B samples of `in` and writes the first span samples
+ * of each result into `out` at b B, adding where two blocks meet (output t
+ * with t mod B < span - B, which the caller zeroes first). The caller
  * launches it only when span <= 2 B (at most two additions per sample, so
  * the result does not depend on their order). */
 int fgk_static_ola_variant(uint32_t modulation, uint32_t L);

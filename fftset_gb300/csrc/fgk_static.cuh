@@ -780,14 +780,16 @@ __device__ __forceinline__ void pp_transform(int tid, int g, float2 *buf0, float
 /* ---- overlap-add, fused into the convolution ---------------------------
  * Block b of a real signal (FREQ_OFFSET_REAL): its first stage reads the
  * signal at b B directly, zero past B samples (or past the signal's end), so
- * the zero-padded blocks are never written out; its last stage adds the
+ * the zero-padded blocks are never written out; its last stage writes the
  * first span = B + K - 1 samples of the block's result into the output at
- * b B with atomicAdd. The host launches this only when span <= 2 B: every
- * output sample then receives at most two additions into a zeroed output,
- * and floating-point addition of two terms does not depend on their order,
- * so the result is deterministic and equals the unfused split / convolution
- * / gather bit for bit. The compiled ping-pong configurations with constant
- * modulation (MODC) provide the stages. */
+ * b B. The host launches this only when span <= 2 B, so output t has one
+ * contributor unless t mod B < K - 1, where block t/B and the block before
+ * it meet: there (the block's first K - 1 and its last span - B samples) the
+ * result is added with atomicAdd into an output the host has zeroed, and
+ * elsewhere stored. Zero plus one term, or two terms in either order, are
+ * exact and order-free, so the result is deterministic and equals the
+ * unfused split / convolution / gather bit for bit. The compiled ping-pong
+ * configurations with constant modulation (MODC) provide the stages. */
 struct OlaArgs {
 	const float *in;      /* the signal, n samples */
 	uint64_t     n;
@@ -795,7 +797,7 @@ struct OlaArgs {
 	uint32_t     nblocks;
 	uint64_t     nout;    /* n + K - 1 */
 	const float *kern;
-	float       *out;     /* zero when the launch starts */
+	float       *out;     /* zero in the overlap zones (t mod B < K - 1) when the launch starts */
 };
 
 /* the zero-padded block as the first stage reads it */
@@ -829,6 +831,7 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_ola(const fgk_pla
 		const uint64_t base = t * a.B;
 		const OlaLoad first{a.in + base, base + a.B <= a.n ? a.B : (uint32_t)(a.n - base)};
 		const uint32_t lim = base + a.span <= a.nout ? a.span : (uint32_t)(a.nout - base);
+		const uint32_t ovl = a.span - a.B; /* K - 1 */
 		float *y = a.out + base;
 		const Ex<C> b0{buf0};
 		pp_first_modc<C, FGK_OP_CONV>(tid, first, mods, [&](int i, float2 v) { b0.put(i, v); });
@@ -883,10 +886,19 @@ __global__ void __launch_bounds__(C::T *C::G, 1) static_kernel_ola(const fgk_pla
 #pragma unroll
 					for (int q = 0; q < RL; q++) {
 						const uint32_t i0 = (uint32_t)(j + q * NBFL), i1 = i0 + (uint32_t)L;
-						if (i0 < lim)
-							atomicAdd(y + i0, v[q].x);
-						if (i1 < lim)
-							atomicAdd(y + i1, v[q].y);
+						/* an overlap zone: the first K - 1 samples and those from B on */
+						if (i0 < lim) {
+							if (i0 < ovl || i0 >= a.B)
+								atomicAdd(y + i0, v[q].x);
+							else
+								stcs(y + i0, v[q].x);
+						}
+						if (i1 < lim) {
+							if (i1 < ovl || i1 >= a.B)
+								atomicAdd(y + i1, v[q].y);
+							else
+								stcs(y + i1, v[q].y);
+						}
 					}
 				}
 			}
