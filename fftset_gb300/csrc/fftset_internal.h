@@ -108,9 +108,10 @@ struct fs_impl {
 	struct fftset_fft *first;
 	/* recursive: held around everything that touches state shared by the
 	 * execution calls of this fftset (staging buffers, the task lists and
-	 * on-demand tables of plans beyond the shared-memory limit), so that
-	 * those calls are thread-safe like the reference's (README.md:38);
-	 * resident-size calls share nothing and do not take it */
+	 * on-demand tables of plans beyond the shared-memory limit, the call
+	 * service's request page), so that those calls are thread-safe like the
+	 * reference's (README.md:38); batched and non-blocking resident-size
+	 * calls share nothing and do not take it */
 	pthread_mutex_t    lock;
 	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
 	uint32_t           spin_limit; /* polls of a task kernel's bounded waits (fgk_launch_tasks) */
