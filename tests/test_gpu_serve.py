@@ -185,3 +185,26 @@ def test_dependent_launch_chain(fftset_lib, mod, L):
         assert O.rel_l2(dh.cpu().numpy(), wh) <= 4 * O.tolerance(2 * L if mod else L)
     finally:
         S.close()
+
+
+@pytest.mark.parametrize("mod,L", [(0, 1024), (1, 1536), (0, 2048), (1, 45)])
+def test_served_calls_in_place(fftset_lib, mod, L):
+    """Blocking single calls with the output buffer equal to the input (as
+    the reference allows) give the batched in-place results bit for bit."""
+    import torch
+    S = fftset_lib.FftSet()
+    try:
+        f = S.create_fft(mod, L)
+        rng = np.random.default_rng(L + 17)
+        B = 10
+        x_np = rng.standard_normal((B, 2 * L)).astype(np.float32)
+        for op in ("forward", "inverse"):
+            want = torch.from_numpy(x_np).cuda()
+            getattr(f, op + "_batch")(want, want)
+            got = torch.from_numpy(x_np).cuda()
+            for b in range(B):
+                getattr(f, op)(got[b], got[b])
+            assert np.array_equal(got.cpu().numpy(), want.cpu().numpy()), op
+        S.check()
+    finally:
+        S.close()
