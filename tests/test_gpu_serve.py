@@ -208,3 +208,47 @@ def test_served_calls_in_place(fftset_lib, mod, L):
         S.check()
     finally:
         S.close()
+
+
+def test_service_setup_failure_falls_back(fftset_lib):
+    """The call service's page cannot be allocated (the allocation wrappers'
+    failure hook): blocking calls run the usual way, with the same results,
+    no latched error, and nothing left allocated after destroy."""
+    import torch
+    H = _hooks(fftset_lib)
+    L_ = fftset_lib.library()
+    L_.fftset__test_fail_allocation.restype = C.c_long
+    L_.fftset__test_fail_allocation.argtypes = [C.c_long]
+    L_.fftset__test_live_allocations.restype = None
+    L_.fftset__test_live_allocations.argtypes = [C.POINTER(C.c_long), C.POINTER(C.c_long)]
+
+    def live():
+        h, d = C.c_long(0), C.c_long(0)
+        L_.fftset__test_live_allocations(C.byref(h), C.byref(d))
+        return h.value, d.value
+
+    L = 1024
+    rng = np.random.default_rng(23)
+    x = torch.from_numpy(rng.standard_normal((6, 2 * L)).astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    base = live()
+    S = fftset_lib.FftSet()
+    try:
+        f = S.create_fft(0, L)
+        want = torch.empty_like(x)
+        f.forward_batch(want, x)
+        got = torch.empty_like(x)
+        f.forward(got[0], x[0])  # the first call of its kind: no service yet
+        L_.fftset__test_fail_allocation(1)  # the service's page is the next allocation
+        try:
+            for b in range(1, 6):
+                f.forward(got[b], x[b])
+        finally:
+            L_.fftset__test_fail_allocation(0)
+        assert np.array_equal(got.cpu().numpy(), want.cpu().numpy())
+        assert H.fftset__test_served_calls(S.handle) == 0
+        S.check()
+    finally:
+        S.close()
+    torch.cuda.synchronize()
+    assert live() == base
