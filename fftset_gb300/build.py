@@ -19,9 +19,9 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["fgk_resident.cu", "fgk_static.cu", "fgk_static_1536.cu", "fgk_static_4096.cu", "fgk_static_1024.cu", "fgk_static_complex.cu", "fgk_fourstep.cu", "fgk_tasks.cu", "fgk_tasks_fc.cu", "fgk_tasks_ff.cu", "fgk_tasks_ic.cu", "fgk_tasks_if.cu", "fgk_tasks_fcw.cu", "fgk_tasks_ffw.cu", "fgk_tasks_icw.cu", "fgk_tasks_ifw.cu", "fgk_fixed_scratch.cu", "fgk_adjoint.cu", "fgk_ola.cu"]
+CU_SOURCES = ["fgk_resident.cu", "fgk_static.cu", "fgk_static_1536.cu", "fgk_static_4096.cu", "fgk_static_1024.cu", "fgk_static_complex.cu", "fgk_fourstep.cu", "fgk_tasks.cu", "fgk_tasks_fc.cu", "fgk_tasks_ff.cu", "fgk_tasks_ic.cu", "fgk_tasks_if.cu", "fgk_tasks_fcw.cu", "fgk_tasks_ffw.cu", "fgk_tasks_icw.cu", "fgk_tasks_ifw.cu", "fgk_tasks_fcs.cu", "fgk_tasks_ffs.cu", "fgk_tasks_ics.cu", "fgk_tasks_ifs.cu", "fgk_fixed_scratch.cu", "fgk_adjoint.cu", "fgk_ola.cu"]
 C_SOURCES = ["fftset_alloc.c", "fftset_host.c", "fftset_layout.c", "fgk_plan.c", "fftset_ragged.c", "fftset_adjoint.c", "fftset_ola.c", "fftset_tuning.c"]
-HEADERS = ["fgk.h", "fgk_codelets.cuh", "fftset_layout.h", "fgk_static.cuh", "fftset_internal.h", "fgk_pingpong.cuh", "fgk_tasks.cuh"]
+HEADERS = ["fgk.h", "fgk_codelets.cuh", "fftset_layout.h", "fgk_static.cuh", "fftset_internal.h", "fgk_pingpong.cuh", "fgk_tasks.cuh", "fgk_serve.cuh"]
 
 
 def _digest(paths, flags):

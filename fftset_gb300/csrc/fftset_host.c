@@ -1342,7 +1342,7 @@ unsigned long long fftset__test_served_calls(struct fftset *fc)
 int fftset__test_set_task_shape(struct fftset *fc, int shape)
 {
 	struct fs_impl *fs = fs_of(fc);
-	if (!fs || shape < -1 || shape > 1)
+	if (!fs || shape < -1 || shape > FGK_SHAPE_SINGLE)
 		return FFTSET_E_INVALID;
 	fs->task_shape = shape;
 	return FFTSET_OK;

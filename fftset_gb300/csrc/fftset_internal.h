@@ -115,7 +115,7 @@ struct fs_impl {
 	pthread_mutex_t    lock;
 	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
 	uint32_t           spin_limit; /* polls of a task kernel's bounded waits (fgk_launch_tasks) */
-	int                task_shape; /* ragged task CTAs: -1 by the list, 0 narrow, 1 wide */
+	int                task_shape; /* ragged task CTAs: -1 by the list, else enum fgk_task_shape */
 	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
@@ -185,7 +185,9 @@ int  fftset__test_set_spin_limit(struct fftset *fc, unsigned polls);
 int  fftset__test_set_call_service(struct fftset *fc, unsigned idle_polls);
 unsigned long long fftset__test_served_calls(struct fftset *fc);
 /* CTA shape of the task lists of later ragged creates: -1 chosen by the
- * list (wide when it holds three-level items), 0 narrow, 1 wide */
+ * list (three-level items: single-buffer when every chain has two stages
+ * at most, else wide; otherwise narrow), or an enum fgk_task_shape (single
+ * makes creates of lists with longer chains fail) */
 int  fftset__test_set_task_shape(struct fftset *fc, int shape);
 int  fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind);
 #if !defined(FS_ALLOC_IMPL) && !defined(__cplusplus)

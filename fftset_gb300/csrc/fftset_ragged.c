@@ -27,14 +27,14 @@
 #include "fgk.h"
 
 /* threads of a narrow task CTA: per-size thread counts (tuned or not) stay
- * within it, so they fit both CTA shapes */
+ * within it, so they fit every CTA shape */
 #define FSR_THREADS ((uint32_t)fgk_tasks_threads(0))
 
 struct fftset_ragged {
 	struct fs_impl *fs;
 	int             op;
 	int             modulation; /* FGK_MOD_* */
-	int             wide;       /* CTA shape: 1 when the list has three-level items */
+	int             shape;      /* CTA shape (enum fgk_task_shape) */
 	unsigned        n;
 	fgk_task       *tasks_dev;
 	uint32_t        ntasks;
@@ -145,6 +145,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	fgk_huge *huges = NULL;
 	fgk_task *tasks = NULL;
 	unsigned i, j, nplans = 0, nitems = 0, nbig = 0, nhuge = 0, ntasks = 0, cap_tasks = 0;
+	uint32_t max_stages = 0; /* the longest chain of any tile of the list */
 	size_t scratch_f2 = 0;
 	uint64_t total_cols = 0;
 	cudaError_t e;
@@ -180,10 +181,13 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		order[i].idx = i;
 		rb->bytes += 16.0 * bins[i];
 		if (bins[i] > 65536)
-			rb->wide = 1; /* three-level items measured faster on wide CTAs */
+			/* three-level items measured fastest on six single-buffer CTAs
+			 * per SM (wide ones when a chain has more than two stages,
+			 * decided once the plans are known below) */
+			rb->shape = FGK_SHAPE_SINGLE;
 	}
 	if (fs->task_shape >= 0)
-		rb->wide = fs->task_shape;
+		rb->shape = fs->task_shape;
 	qsort(order, n, sizeof(*order), fsr_cmp);
 
 	/* plans, items and big items; SMALL tasks are counted here, listed below */
@@ -199,11 +203,13 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		if (!f->fourstep && L <= (uint32_t)fgk_tasks_points()) {
 			const fgk_plan *pl = f->rg_tuned && f->rg_dmem ? &f->rg_plan : &f->rp;
 			const uint32_t tg = f->rg_tuned ? f->rg_tg : fsr_item_threads(pl);
-			uint32_t G = (uint32_t)fgk_tasks_threads(rb->wide) / tg;
+			uint32_t G = (uint32_t)fgk_tasks_threads(rb->shape) / tg;
 			if (!pl->fwd.code) { /* tiles take chains of at most 15 stages */
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
 			}
+			if (pl->fwd.nstages > max_stages)
+				max_stages = pl->fwd.nstages;
 			if (G * fsr_slots(L) > (uint32_t)fgk_tasks_slots())
 				G = (uint32_t)fgk_tasks_slots() / fsr_slots(L);
 			plans[nplans] = *pl;
@@ -221,6 +227,11 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			if (!p3->c1.code || !p3->c2.code || !p3->c3.code) {
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
+			}
+			for (k = 0; k < 3; k++) {
+				const uint32_t ns = (k == 0 ? p3->c1 : k == 1 ? p3->c2 : p3->c3).nstages;
+				if (ns > max_stages)
+					max_stages = ns;
 			}
 			for (k = i; k < j; k++) {
 				fgk_huge *h = &huges[nhuge++];
@@ -257,6 +268,10 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 				rc = FFTSET_E_UNSUPPORTED;
 				goto fail;
 			}
+			if (f->p4.c1.nstages > max_stages)
+				max_stages = f->p4.c1.nstages;
+			if (f->p4.c2.nstages > max_stages)
+				max_stages = f->p4.c2.nstages;
 			for (k = i; k < j; k++) {
 				fgk_big *b = &bigs[nbig++];
 				b->p4 = f->p4.dev;
@@ -277,6 +292,15 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 				scratch_f2 += ((((size_t)b->nrows * L2) << b->ls2) + 15) & ~(size_t)15;
 			}
 		}
+	}
+	/* one tile buffer holds chains of two stages only; the SMALL tasks were
+	 * packed for 128 threads, which the wide shape's CTAs run as well */
+	if (rb->shape == FGK_SHAPE_SINGLE && max_stages > 2) {
+		if (fs->task_shape == FGK_SHAPE_SINGLE) {
+			rc = FFTSET_E_UNSUPPORTED;
+			goto fail;
+		}
+		rb->shape = FGK_SHAPE_WIDE;
 	}
 	tasks = (fgk_task *)malloc(sizeof(*tasks) * (cap_tasks ? cap_tasks : 1));
 	if (!tasks)
@@ -305,7 +329,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	}
 	/* big items: COLS of item b, ROWS of item b - D */
 	if (nbig) {
-		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms, rb->wide);
+		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms, rb->shape);
 		const uint64_t avg = (total_cols + nbig - 1) / nbig;
 		uint32_t D = (uint32_t)((2 * grid + avg - 1) / avg) + 1, b, t;
 		for (b = 0; b < nbig + D; b++) {
@@ -421,7 +445,7 @@ static int fsr_record_product(struct fftset_ragged *rb, int op, float *out, cons
 	const fgk_product none = {NULL};
 	return fgk_launch_tasks(rb->tasks_dev, rb->ntasks, rb->plans_dev, rb->items_dev, rb->bigs_dev, rb->nbig,
 	                        rb->huges_dev, rb->nhuge, rb->counters_dev, rb->scratch, op, rb->modulation, in, out,
-	                        fs->num_sms, rb->wide, fs->dev_flag, fs->spin_limit, prod ? *prod : none, s);
+	                        fs->num_sms, rb->shape, fs->dev_flag, fs->spin_limit, prod ? *prod : none, s);
 }
 
 static int fsr_record(struct fftset_ragged *rb, int op, float *out, const float *in, cudaStream_t s)

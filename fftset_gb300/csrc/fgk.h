@@ -203,15 +203,20 @@ int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in,
  * each three-level item) and is reset by the launcher;
  * scratch_dev holds the big items' L1 x L2 intermediates; err_flag is set
  * when a bounded wait gives up, after spin_limit polls (about 256 ns
- * apart); wide selects the CTA shape the list was planned for (0: 128
- * threads, three CTAs per SM; 1: 256 threads, two) */
+ * apart); shape selects the CTA shape the list was planned for (enum
+ * fgk_task_shape) */
+enum fgk_task_shape {
+	FGK_SHAPE_NARROW = 0, /* 128 threads, two tile buffers, three CTAs per SM */
+	FGK_SHAPE_WIDE = 1,   /* 256 threads, two buffers, three CTAs per SM */
+	FGK_SHAPE_SINGLE = 2  /* 128 threads, one buffer, six CTAs per SM: chains of two stages at most */
+};
 int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                         const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                         const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev,
                         float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
-                        int num_sms, int wide, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream);
-int    fgk_tasks_grid(int num_sms, int wide);
-int    fgk_tasks_threads(int wide);
+                        int num_sms, int shape, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream);
+int    fgk_tasks_grid(int num_sms, int shape);
+int    fgk_tasks_threads(int shape);
 /* points of a tile (items up to this size run whole) and the shared-memory
  * slots of one of its two buffers */
 int    fgk_tasks_points(void);

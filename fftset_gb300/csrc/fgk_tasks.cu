@@ -33,6 +33,10 @@ extern "C" int fgk_launch_tasks_fcw(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ffw(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_icw(FGKT_LAUNCH_ARGS);
 extern "C" int fgk_launch_tasks_ifw(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_fcs(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_ffs(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_ics(FGKT_LAUNCH_ARGS);
+extern "C" int fgk_launch_tasks_ifs(FGKT_LAUNCH_ARGS);
 
 extern "C" int fgk_tasks_points(void)
 {
@@ -44,21 +48,26 @@ extern "C" int fgk_tasks_slots(void)
 	return fgk::TK_SLOTS;
 }
 
-extern "C" int fgk_tasks_threads(int wide)
+extern "C" int fgk_tasks_threads(int shape)
 {
-	return wide ? fgk::TK_THREADS_WIDE : fgk::TK_THREADS_NARROW;
+	return shape == FGK_SHAPE_WIDE ? fgk::TK_THREADS_WIDE
+	       : shape == FGK_SHAPE_SINGLE ? fgk::TK_THREADS_SINGLE
+	                                   : fgk::TK_THREADS_NARROW;
 }
 
-extern "C" int fgk_tasks_grid(int num_sms, int wide)
+extern "C" int fgk_tasks_grid(int num_sms, int shape)
 {
-	return (wide ? fgk::TK_CTAS_WIDE : fgk::TK_CTAS_NARROW) * num_sms;
+	return (shape == FGK_SHAPE_WIDE     ? fgk::TK_CTAS_WIDE
+	        : shape == FGK_SHAPE_SINGLE ? fgk::TK_CTAS_SINGLE
+	                                    : fgk::TK_CTAS_NARROW) *
+	       num_sms;
 }
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
                                 const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev, float *scratch_dev,
                                 int op, int modulation, const float *in_base, float *out_base, int num_sms,
-                                int wide, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream)
+                                int shape, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream)
 {
 	const bool inv = op == FGK_OP_INVERSE, freq = modulation == FGK_MOD_FREQOFF;
 	cudaStream_t s = (cudaStream_t)stream;
@@ -68,15 +77,19 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig + 2 * (size_t)nhuge), s)) !=
 	    cudaSuccess)
 		return (int)e;
-	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms, wide);
+	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms, shape);
 	if (grid > ntasks)
 		grid = ntasks;
 	int *hcounters = counters_dev + 1 + nbig;
 	float2 *scratch = reinterpret_cast<float2 *>(scratch_dev);
-	auto launch = wide ? (inv ? (freq ? fgk_launch_tasks_ifw : fgk_launch_tasks_icw)
-	                          : (freq ? fgk_launch_tasks_ffw : fgk_launch_tasks_fcw))
-	                   : (inv ? (freq ? fgk_launch_tasks_if : fgk_launch_tasks_ic)
-	                          : (freq ? fgk_launch_tasks_ff : fgk_launch_tasks_fc));
+	auto launch = shape == FGK_SHAPE_WIDE
+	                  ? (inv ? (freq ? fgk_launch_tasks_ifw : fgk_launch_tasks_icw)
+	                         : (freq ? fgk_launch_tasks_ffw : fgk_launch_tasks_fcw))
+	              : shape == FGK_SHAPE_SINGLE
+	                  ? (inv ? (freq ? fgk_launch_tasks_ifs : fgk_launch_tasks_ics)
+	                         : (freq ? fgk_launch_tasks_ffs : fgk_launch_tasks_fcs))
+	                  : (inv ? (freq ? fgk_launch_tasks_if : fgk_launch_tasks_ic)
+	                         : (freq ? fgk_launch_tasks_ff : fgk_launch_tasks_fc));
 	return launch(grid, tasks_dev, ntasks, plans_dev, items_dev, bigs_dev, huges_dev, counters_dev, hcounters, scratch,
 	              in_base, out_base, err_flag, spin_limit, prod, s);
 }

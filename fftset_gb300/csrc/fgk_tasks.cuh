@@ -55,6 +55,14 @@ namespace fgk {
  * 0.641 on two wide CTAs per SM, with no spills, and 0.684 narrow). */
 constexpr int TK_THREADS_NARROW = 128, TK_CTAS_NARROW = 3;
 constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 3;
+/* A third shape for lists whose every chain has at most two stages (the
+ * first stage writes buffer A and the last reads it, so B is never used):
+ * 128 threads, one buffer, six CTAs (six tiles in flight) per SM, 80
+ * registers with a few hundred bytes of spills. The 15,728,640-bin
+ * forward + inverse (240 x 256 x 256, all two-stage): 0.534 ms against
+ * 0.604 on the wide shape. A task whose chain is longer is refused (error
+ * flag) rather than run on one buffer; the host never lists one. */
+constexpr int TK_THREADS_SINGLE = 128, TK_CTAS_SINGLE = 6;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
 constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
 
@@ -671,7 +679,7 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 /* One CTA: run tasks in claim order. Thread 0 claims the next task as the
  * current one starts, so the claim's round trip overlaps the work. One
  * instantiation per (direction, modulation): a batch has one of each. */
-template <bool inverse, bool freq, int THREADS, int MINB>
+template <bool inverse, bool freq, int THREADS, int MINB, int BUFS>
 __global__ void __launch_bounds__(THREADS, MINB)
     task_kernel(const fgk_task *__restrict__ tasks, uint32_t ntasks, const fgk_plan *__restrict__ plans,
                 const fgk_rg_item *__restrict__ items, const fgk_big *__restrict__ bigs,
@@ -713,7 +721,22 @@ __global__ void __launch_bounds__(THREADS, MINB)
 		int *count = nullptr; /* the tile's counter, released after the barrier below */
 		if (threadIdx.x == 0)
 			ahead = (uint32_t)atomicAdd(counters, 1);
-		if (tk.kind == FGK_TASK_SMALL)
+		bool fits = true;
+		if constexpr (BUFS == 1) {
+			/* one buffer holds two-stage chains only */
+			const uint64_t code = tk.kind == FGK_TASK_SMALL  ? plans[tk.ref].fwd.code
+			                      : tk.kind == FGK_TASK_COLS ? bigs[tk.ref].code1
+			                      : tk.kind == FGK_TASK_ROWS ? bigs[tk.ref].code2
+			                      : tk.kind == FGK_TASK_PA   ? huges[tk.ref].code1
+			                      : tk.kind == FGK_TASK_PB   ? huges[tk.ref].code2
+			                                                 : huges[tk.ref].code3;
+			fits = (code & 15) <= 2;
+			if (!fits && threadIdx.x == 0)
+				atomicExch(err, 1);
+		}
+		if (!fits) {
+			/* refused, the error flag raised */
+		} else if (tk.kind == FGK_TASK_SMALL)
 			task_small<inverse, freq>(tk, plans, items, in_base, out_base, smem, pre);
 		else if (tk.kind == FGK_TASK_COLS)
 			count = task_cols<inverse, freq>(tk, bigs[tk.ref], in_base, scratch, counters + 1 + tk.ref, smem, pre);
@@ -753,22 +776,21 @@ __global__ void __launch_bounds__(THREADS, MINB)
 }
 
 /* Launch of one instantiation (each lives in its own translation unit,
- * fgk_tasks_<direction><modulation>[w].cu, so that the eight compile in
+ * fgk_tasks_<direction><modulation>[w|s].cu, so that the twelve compile in
  * parallel); counters are already zeroed. */
-template <bool inverse, bool freq, int THREADS, int MINB>
+template <bool inverse, bool freq, int THREADS, int MINB, int BUFS = 2>
 int launch_tasks(uint32_t grid, const fgk_task *tasks, uint32_t ntasks, const fgk_plan *plans,
                  const fgk_rg_item *items, const fgk_big *bigs, const fgk_huge *huges, int *counters,
                  int *hcounters, float2 *scratch, const float *in_base, float *out_base, int *err, uint32_t spin_limit,
                  fgk_product prod, cudaStream_t stream)
 {
-	const size_t smem = 2 * (size_t)TK_SLOTS * sizeof(float2);
-	cudaError_t e = cudaFuncSetAttribute((const void *)task_kernel<inverse, freq, THREADS, MINB>,
-	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	const size_t smem = (size_t)BUFS * TK_SLOTS * sizeof(float2);
+	auto kern = task_kernel<inverse, freq, THREADS, MINB, BUFS>;
+	cudaError_t e = cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 	if (e != cudaSuccess)
 		return (int)e;
-	task_kernel<inverse, freq, THREADS, MINB><<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters,
-	                                                              hcounters, scratch, in_base, out_base, err,
-	                                                              spin_limit, prod);
+	kern<<<grid, THREADS, smem, stream>>>(tasks, ntasks, plans, items, bigs, huges, counters, hcounters, scratch, in_base,
+	                                      out_base, err, spin_limit, prod);
 	fgk_count_launch();
 	return (int)cudaGetLastError();
 }

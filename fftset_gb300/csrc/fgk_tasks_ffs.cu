@@ -1,0 +1,7 @@
+/* The ragged task kernel (forward, FREQ_OFFSET_REAL), single-buffer CTAs; fgk_tasks.cuh. */
+#include "fgk_tasks.cuh"
+
+extern "C" int fgk_launch_tasks_ffs(FGKT_LAUNCH_ARGS)
+{
+	return fgk::launch_tasks<false, true, fgk::TK_THREADS_SINGLE, fgk::TK_CTAS_SINGLE, 1>(FGKT_LAUNCH_PASS);
+}

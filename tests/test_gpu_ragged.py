@@ -108,8 +108,46 @@ def test_ragged_both_task_shapes(fftset_lib, mod):
                     want = O.forward64(mod, xi) if op == fftset_lib.OP_FORWARD else O.inverse64(mod, xi)
                     assert O.rel_l2(yh[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (shape, L, op)
                 rb.close()
-        assert L_.fftset__test_set_task_shape(S.handle, 2) != 0
+        assert L_.fftset__test_set_task_shape(S.handle, 3) != 0
         S.check()
+    finally:
+        S.close()
+
+
+@pytest.mark.parametrize("mod", [0, 1])
+def test_ragged_single_buffer_shape(fftset_lib, mod):
+    """The single-buffer CTA shape (six per SM, one tile buffer) on a list
+    whose every chain has two stages (items up to 256 bins, two-level and
+    three-level items with such factors): every item against FP64; a list
+    with a longer chain is refused on that shape."""
+    import ctypes as C
+    import torch
+    L_ = fftset_lib.library()
+    L_.fftset__test_set_task_shape.restype = C.c_int
+    L_.fftset__test_set_task_shape.argtypes = [fftset_lib._P, C.c_int]
+    sizes = [262144, 65536, 61440, 16384, 256, 240, 128, 96, 60, 64, 200, 256, 16, 12]
+    sizes = [s for s in sizes if O.valid_size(s)]
+    offs, total = layout(sizes)
+    x = np.random.default_rng(31).uniform(-1, 1, total).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    S = fftset_lib.FftSet()
+    try:
+        assert L_.fftset__test_set_task_shape(S.handle, 2) == 0
+        for op in (fftset_lib.OP_FORWARD, fftset_lib.OP_INVERSE):
+            rb = fftset_lib.Ragged(S, mod, op, sizes, offs, offs)
+            y = torch.full_like(xd, 3.0)
+            rb.execute(y, xd)
+            torch.cuda.synchronize()
+            yh = y.cpu().numpy()
+            for L, o in zip(sizes, offs):
+                xi = x[o:o + 2 * L]
+                want = O.forward64(mod, xi) if op == fftset_lib.OP_FORWARD else O.inverse64(mod, xi)
+                assert O.rel_l2(yh[o:o + 2 * L], want) <= O.tolerance(2 * L if mod else L), (L, op)
+            rb.close()
+        S.check()
+        with pytest.raises(fftset_lib.FftsetError):  # 4096 = 16 x 16 x 16: three stages
+            fftset_lib.Ragged(S, mod, fftset_lib.OP_FORWARD, [4096, 256], [0, 8192], [0, 8192])
+        S.clear_error()
     finally:
         S.close()
 
