@@ -146,6 +146,7 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	fgk_task *tasks = NULL;
 	unsigned i, j, nplans = 0, nitems = 0, nbig = 0, nhuge = 0, ntasks = 0, cap_tasks = 0;
 	uint32_t max_stages = 0; /* the longest chain of any tile of the list */
+	int three_level = 0;
 	size_t scratch_f2 = 0;
 	uint64_t total_cols = 0;
 	cudaError_t e;
@@ -181,13 +182,12 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		order[i].idx = i;
 		rb->bytes += 16.0 * bins[i];
 		if (bins[i] > 65536)
-			/* three-level items measured fastest on six single-buffer CTAs
-			 * per SM (wide ones when a chain has more than two stages,
-			 * decided once the plans are known below) */
-			rb->shape = FGK_SHAPE_SINGLE;
+			three_level = 1;
 	}
-	if (fs->task_shape >= 0)
-		rb->shape = fs->task_shape;
+	/* the shape is settled once the plans (their chains) are known below;
+	 * the SMALL tasks are packed for 128-thread CTAs meanwhile, which every
+	 * shape runs */
+	rb->shape = fs->task_shape >= 0 ? fs->task_shape : FGK_SHAPE_NARROW;
 	qsort(order, n, sizeof(*order), fsr_cmp);
 
 	/* plans, items and big items; SMALL tasks are counted here, listed below */
@@ -293,14 +293,16 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 			}
 		}
 	}
-	/* one tile buffer holds chains of two stages only; the SMALL tasks were
-	 * packed for 128 threads, which the wide shape's CTAs run as well */
-	if (rb->shape == FGK_SHAPE_SINGLE && max_stages > 2) {
-		if (fs->task_shape == FGK_SHAPE_SINGLE) {
-			rc = FFTSET_E_UNSUPPORTED;
-			goto fail;
-		}
-		rb->shape = FGK_SHAPE_WIDE;
+	/* Chains of two stages at most run on six single-buffer CTAs per SM
+	 * (the 15,728,640-bin pair: 0.529 against 0.604 ms on wide CTAs; the
+	 * mix's two-stage two-level items: 0.775 against 0.820 ms on narrow
+	 * ones); otherwise three-level lists on wide CTAs, the rest on narrow
+	 * ones. One tile buffer cannot hold a longer chain. */
+	if (fs->task_shape < 0)
+		rb->shape = max_stages <= 2 ? FGK_SHAPE_SINGLE : three_level ? FGK_SHAPE_WIDE : FGK_SHAPE_NARROW;
+	else if (rb->shape == FGK_SHAPE_SINGLE && max_stages > 2) {
+		rc = FFTSET_E_UNSUPPORTED;
+		goto fail;
 	}
 	tasks = (fgk_task *)malloc(sizeof(*tasks) * (cap_tasks ? cap_tasks : 1));
 	if (!tasks)
