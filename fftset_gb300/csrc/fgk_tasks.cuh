@@ -2,9 +2,9 @@
  *
  * Every task is a tile of at most FGKT_POINTS points held in two padded
  * shared-memory buffers (ping-pong Stockham stages, one butterfly per thread
- * at a time, runtime radix; fgk_pingpong.cuh), 70 KB per CTA; a CTA has 128
- * threads (three CTAs per SM) or 256 (two per SM), see TK_THREADS_NARROW.
- * Loads are issued eight per thread before any is used.
+ * at a time, runtime radix; fgk_pingpong.cuh), 70 KB per CTA, or in one
+ * buffer when every chain of the list has two stages; the CTA shapes are
+ * described at TK_THREADS_NARROW.
  *
  *   SMALL  n items of one size L <= FGKT_POINTS, whole transforms side
  *          by side (tg threads each), HBM in, HBM out.
@@ -46,22 +46,25 @@ namespace fgk {
 #ifndef FGKT_POINTS
 #define FGKT_POINTS 4096 /* points of a tile */
 #endif
-/* Two CTA shapes, chosen per task list, both three CTAs (three tiles) per
- * SM: narrow, 128 threads (up to 168 registers a thread, no spills), for
- * lists of items up to 65536 bins (the 20000-item ragged mix: 1.757 ms
+/* CTA shapes, chosen per task list (fgk.h, enum fgk_task_shape). Narrow
+ * and wide have two tile buffers and three CTAs (three tiles) per SM:
+ * narrow, 128 threads (up to 168 registers a thread, no spills), for lists
+ * with chains of three stages or more (the 20000-item ragged mix: 1.757 ms
  * against 1.851 on two wide CTAs per SM and 1.90 on three); wide, 256
- * threads (80 registers, a few hundred bytes of spills), for lists with
- * three-level items (the 15,728,640-bin forward + inverse: 0.604 ms against
- * 0.641 on two wide CTAs per SM, with no spills, and 0.684 narrow). */
+ * threads (80 registers, a few hundred bytes of spills), for such lists
+ * with three-level items (the 15,728,640-bin forward + inverse on it: 0.604
+ * ms against 0.641 on two wide CTAs per SM, with no spills, and 0.684
+ * narrow). */
 constexpr int TK_THREADS_NARROW = 128, TK_CTAS_NARROW = 3;
 constexpr int TK_THREADS_WIDE = 256, TK_CTAS_WIDE = 3;
 /* A third shape for lists whose every chain has at most two stages (the
  * first stage writes buffer A and the last reads it, so B is never used):
  * 128 threads, one buffer, six CTAs (six tiles in flight) per SM, 80
  * registers with a few hundred bytes of spills. The 15,728,640-bin
- * forward + inverse (240 x 256 x 256, all two-stage): 0.534 ms against
- * 0.604 on the wide shape. A task whose chain is longer is refused (error
- * flag) rather than run on one buffer; the host never lists one. */
+ * forward + inverse (240 x 256 x 256, all two-stage): 0.53 ms against 0.604
+ * on the wide shape; the 65536-bin convolution batch 0.60 against 0.70 ms
+ * on the narrow one. A task whose chain is longer is refused (error flag)
+ * rather than run on one buffer; the host never lists one. */
 constexpr int TK_THREADS_SINGLE = 128, TK_CTAS_SINGLE = 6;
 /* float2 slots of one of the two tile buffers: rslots(points), rounded up to 4 */
 constexpr int TK_SLOTS = (FGKT_POINTS + FGKT_POINTS / 16 + 1 + 3) & ~3;
