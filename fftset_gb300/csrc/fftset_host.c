@@ -1348,6 +1348,15 @@ int fftset__test_set_task_shape(struct fftset *fc, int shape)
 	return FFTSET_OK;
 }
 
+int fftset__test_set_group_distance(struct fftset *fc, unsigned slots)
+{
+	struct fs_impl *fs = fs_of(fc);
+	if (!fs)
+		return FFTSET_E_INVALID;
+	fs->group_dist = slots;
+	return FFTSET_OK;
+}
+
 int fftset_set_blocking(struct fftset *fc, int blocking)
 {
 	struct fs_impl *fs = fs_of(fc);

@@ -116,6 +116,7 @@ struct fs_impl {
 	int               *host_flag; /* mapped pinned int: kernels report a failed bounded wait */
 	uint32_t           spin_limit; /* polls of a task kernel's bounded waits (fgk_launch_tasks) */
 	int                task_shape; /* ragged task CTAs: -1 by the list, else enum fgk_task_shape */
+	uint32_t           group_dist; /* three-level lists: slots from A to B tiles of a group; 0: all A tiles first */
 	int               *dev_flag;
 	void              *stage[FS_NSTAGE];
 	size_t             stage_bytes[FS_NSTAGE];
@@ -189,6 +190,9 @@ unsigned long long fftset__test_served_calls(struct fftset *fc);
  * at most, else wide; otherwise narrow), or an enum fgk_task_shape (single
  * makes creates of lists with longer chains fail) */
 int  fftset__test_set_task_shape(struct fftset *fc, int shape);
+/* slots between the A and the B tiles of an n3 group in the three-level
+ * lists of later ragged creates (0: the default, every A tile first) */
+int  fftset__test_set_group_distance(struct fftset *fc, unsigned slots);
 int  fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind);
 #if !defined(FS_ALLOC_IMPL) && !defined(__cplusplus)
 #include <stdlib.h>

@@ -143,16 +143,22 @@ typedef struct fgk_product {
 int fgk_launch_spectrum_natural(const float *kern, const int32_t *kidx, int kvw, uint32_t L, int conj, void *spec,
                                 void *stream);
 
-/* A three-level item: passes A, B, C through two scratch areas; B tiles
- * wait for every A tile of the item, C tiles for every B tile. */
+/* A three-level item: passes A, B, C through two scratch areas. When 16
+ * divides L3 the A and B tiles fall into ngrp = L3/16 groups by n3 (A tile
+ * t: t % ngrp; B tile: its n3 / 16) and a B tile waits for the L2 A tiles
+ * of its group only; otherwise ngrp = 1 and B tiles wait for every A tile.
+ * A C tile (16 k1) waits for the B tiles of its 16 k1 only. The item's
+ * counters: hcounters[cnt + u], u < ngrp, A tiles done in n3 group u;
+ * hcounters[cnt + ngrp + g], g < nc1, B tiles done in k1 group g. */
 typedef struct fgk_huge {
 	const struct fgk_plan3 *p3;             /* device copy of the item's plan */
-	uint32_t                L1, L2, L3, reserved;
+	uint32_t                L1, L2, L3, ngrp;
 	uint64_t                code1, code2, code3; /* the passes' chains (fgk_chain.code) */
 	uint64_t                in_off, out_off; /* floats from the batch's base pointers */
 	uint64_t                sa, sb;          /* float2 offsets of its A and B scratch */
 	uint32_t                na, nb;          /* A tiles, B tiles */
 	uint32_t                nb3, nc1;        /* B tiles per k1 group (ceil(L3/4)), C tiles per k2 (ceil(L1/16)) */
+	uint32_t                cnt, reserved;   /* first counter of the item */
 } fgk_huge;
 
 typedef struct fgk_big {
@@ -198,9 +204,9 @@ uint32_t fgk_max_resident_L(void);
 int fgk_launch_fourstep(const fgk_plan4 *p, int op, float *out, const float *in, const float *kern,
                         const int32_t *kidx, int kvw, float *work, uint32_t count, size_t in_stride,
                         size_t out_stride, size_t work_stride, void *stream);
-/* the task launch: counters_dev holds 1 + nbig + 2 nhuge ints (claim counter,
- * the finished COLS tiles of each big item, the finished A and B tiles of
- * each three-level item) and is reset by the launcher;
+/* the task launch: counters_dev holds 1 + nbig + nhcount ints (claim
+ * counter, the finished COLS tiles of each big item, the three-level items'
+ * counters, fgk_huge.cnt) and is reset by the launcher;
  * scratch_dev holds the big items' L1 x L2 intermediates; err_flag is set
  * when a bounded wait gives up, after spin_limit polls (about 256 ns
  * apart); shape selects the CTA shape the list was planned for (enum
@@ -212,7 +218,7 @@ enum fgk_task_shape {
 };
 int    fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                         const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
-                        const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev,
+                        const fgk_huge *huges_dev, uint32_t nhcount, int *counters_dev,
                         float *scratch_dev, int op, int modulation, const float *in_base, float *out_base,
                         int num_sms, int shape, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream);
 int    fgk_tasks_grid(int num_sms, int shape);

@@ -65,7 +65,7 @@ extern "C" int fgk_tasks_grid(int num_sms, int shape)
 
 extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, const fgk_plan *plans_dev,
                                 const fgk_rg_item *items_dev, const fgk_big *bigs_dev, uint32_t nbig,
-                                const fgk_huge *huges_dev, uint32_t nhuge, int *counters_dev, float *scratch_dev,
+                                const fgk_huge *huges_dev, uint32_t nhcount, int *counters_dev, float *scratch_dev,
                                 int op, int modulation, const float *in_base, float *out_base, int num_sms,
                                 int shape, int *err_flag, uint32_t spin_limit, fgk_product prod, void *stream)
 {
@@ -74,7 +74,7 @@ extern "C" int fgk_launch_tasks(const fgk_task *tasks_dev, uint32_t ntasks, cons
 	cudaError_t e;
 	if (ntasks == 0)
 		return 0;
-	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig + 2 * (size_t)nhuge), s)) !=
+	if ((e = cudaMemsetAsync(counters_dev, 0, sizeof(int) * (1 + (size_t)nbig + (size_t)nhcount), s)) !=
 	    cudaSuccess)
 		return (int)e;
 	uint32_t grid = (uint32_t)fgk_tasks_grid(num_sms, shape);

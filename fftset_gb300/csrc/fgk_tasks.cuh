@@ -533,10 +533,11 @@ __device__ __forceinline__ uint32_t tk_blk_b(uint32_t k2, uint32_t n3, uint32_t 
 
 /* A: 16 adjacent columns c = n2 L3 + n3, DFT_L1 over n1 straight from the
  * input, times w_{L1 L2}^{n2 k1} = w_{L1 L2}^{n2 j} w_{R1 L2}^{n2 q}, into
- * the blocked A. */
+ * the blocked A. Returns the counter of the tile's group (tile t, columns
+ * 16t .. 16t + 15: n3 group t % ngrp when 16 divides L3). */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, const float *in_base,
-                                        float2 *scratch, int *done, float2 *smem, Pre &&pre)
+                                        float2 *scratch, int *hcounters, float2 *smem, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)hg.L1, L3 = (int)hg.L3;
@@ -581,17 +582,19 @@ __device__ __forceinline__ int *task_pa(const fgk_task &tk, const fgk_huge &hg, 
 	};
 	tile_chain<false, Rows>(hg.code1, L1, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
 	                        (int)blockDim.x, true, ld, st, pre);
-	return done;
+	return hcounters + hg.cnt + tk.a % hg.ngrp;
 }
 
 /* B: a block of 4 k1 x 4 n3 (lanes l -> k1b + l/4, n3b + l%4), DFT_L2 over
  * n2 from the blocked A (one block per n2), times w_L^{n3 (k1 + L1 k2)} =
  * w_L^{n3 (k1 + L1 j)} w_{R2 L3}^{n3 q}, into the blocked B (one block per
- * k2). */
+ * k2). Waits for the A tiles of its n3 group (all A tiles when ngrp = 1)
+ * and counts itself in its group of 16 k1 (the C tiles' unit); every A
+ * block is read by this tile alone, so once the first stage has read them
+ * their L2 lines are dropped without a write-back. */
 template <bool inverse, bool freq, class Pre>
-__device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, const int *done_a,
-                                        int *done_b, int *err, uint32_t spin_limit, float2 *smem, int *failed,
-                                        Pre &&pre)
+__device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, float2 *scratch, int *hcounters,
+                                        int *err, uint32_t spin_limit, float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
 	const int L1 = (int)hg.L1, L2 = (int)hg.L2, L3 = (int)hg.L3;
@@ -603,7 +606,8 @@ __device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, 
 	const float xL = 2.0f / (float)L;
 	const float2 *A = scratch + hg.sa;
 	float2 *B = scratch + hg.sb;
-	if (!tk_wait(done_a, (int)hg.na, err, failed, spin_limit))
+	const uint32_t grp = hg.ngrp > 1 ? (uint32_t)n3b >> 4 : 0;
+	if (!tk_wait(hcounters + hg.cnt + grp, (int)(hg.na / hg.ngrp), err, failed, spin_limit))
 		return nullptr;
 	const uint32_t L1q = hg.nb / hg.nb3, L3q = hg.nb3;
 	auto ld = [&](int n2, int lane) {
@@ -621,17 +625,27 @@ __device__ __forceinline__ int *task_pb(const fgk_task &tk, const fgk_huge &hg, 
 		const float2 w = q ? cmul(b, __ldg(tq + (uint32_t)n3 * (uint32_t)q)) : b;
 		__stcg(B + tk_blk_b((uint32_t)(j + q * nbf), (uint32_t)n3, (uint32_t)k1, L1q, L3q), cmul(v, w));
 	};
+	auto discard = [&] {
+		for (int n2 = (int)threadIdx.x; n2 < L2; n2 += (int)blockDim.x) {
+			const float2 *a = A + tk_blk_a((uint32_t)k1b, (uint32_t)n2, (uint32_t)n3b, L1q, L3q);
+			asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+		}
+	};
 	tile_chain<false, Rows>(hg.code2, L2, 4, smem, smem + TK_SLOTS, (int)threadIdx.x,
-	                        (int)blockDim.x, true, ld, st, pre);
-	return done_b;
+	                        (int)blockDim.x, true, ld, st, [&] {
+		                        discard();
+		                        pre();
+	                        });
+	return hcounters + hg.cnt + hg.ngrp + (k1g >> 2);
 }
 
 /* C: 16 adjacent k1 of one k2, DFT_L3 over n3 from the blocked B (four
  * 32-byte sectors per n3), into X[k1 + L1 k2 + L1 L2 k3] (the modulation's
- * final step fused). */
+ * final step fused). Waits for the B tiles of its 16 k1: their 4 (fewer at
+ * the end) k1 blocks times ceil(L3/4) n3 blocks. */
 template <bool inverse, bool freq, class Pre>
 __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, float *out_base, float2 *scratch,
-                                        const int *done_b, int *err, uint32_t spin_limit, const fgk_product &prod,
+                                        const int *hcounters, int *err, uint32_t spin_limit, const fgk_product &prod,
                                         float2 *smem, int *failed, Pre &&pre)
 {
 	const fgk_plan3 *p = hg.p3;
@@ -643,9 +657,10 @@ __device__ __forceinline__ void task_pc(const fgk_task &tk, const fgk_huge &hg, 
 	float *o = out_base + hg.out_off;
 	float2 *o2 = reinterpret_cast<float2 *>(o);
 	const float2 *oa = (const float2 *)p->oa, *ob = (const float2 *)p->ob, *oc = (const float2 *)p->oc;
-	if (!tk_wait(done_b, (int)hg.nb, err, failed, spin_limit))
-		return;
 	const uint32_t L1q = hg.nb / hg.nb3, L3q = hg.nb3;
+	const uint32_t kg = (uint32_t)k1b >> 4, nblk = min(4u, L1q - 4 * kg);
+	if (!tk_wait(hcounters + hg.cnt + hg.ngrp + kg, (int)(nblk * L3q), err, failed, spin_limit))
+		return;
 	auto ld = [&](int n3, int lane) {
 		const int k1 = k1b + lane;
 		if (k1 >= L1)
@@ -747,13 +762,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
 			task_rows<inverse, freq>(tk, bigs[tk.ref], out_base, scratch, counters + 1 + tk.ref, err, spin_limit,
 			                         prod, smem, &failed, pre);
 		else if (tk.kind == FGK_TASK_PA)
-			count = task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters + 2 * tk.ref, smem, pre);
+			count = task_pa<inverse, freq>(tk, huges[tk.ref], in_base, scratch, hcounters, smem, pre);
 		else if (tk.kind == FGK_TASK_PB)
-			count = task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters + 2 * tk.ref,
-			                               hcounters + 2 * tk.ref + 1, err, spin_limit, smem, &failed, pre);
+			count = task_pb<inverse, freq>(tk, huges[tk.ref], scratch, hcounters, err, spin_limit, smem, &failed,
+			                               pre);
 		else
-			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters + 2 * tk.ref + 1, err, spin_limit,
-			                       prod, smem, &failed, pre);
+			task_pc<inverse, freq>(tk, huges[tk.ref], out_base, scratch, hcounters, err, spin_limit, prod, smem,
+			                       &failed, pre);
 		if (threadIdx.x == 0) {
 			if (copying) {
 				asm volatile("cp.async.wait_all;" ::: "memory");

@@ -383,7 +383,10 @@ def test_radix9_chains_against_fp64(gpu_set, mod, L):
     assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
 
 
-FOURSTEP = [32768, 36864, 46656, 59049, 65536, 131072, 393216]
+# three-level from 131072 on: n3 groups 4 (131072), 6 (393216), 5 (327680, an
+# odd count, so with mirror tiles adjacent the middle group pairs with
+# itself) and one (177147 = 27 x 81 x 81: 16 does not divide L3)
+FOURSTEP = [32768, 36864, 46656, 59049, 65536, 131072, 393216, 327680, 177147]
 
 
 @pytest.mark.parametrize("mod", [0, 1])
@@ -418,6 +421,43 @@ def test_fourstep_sizes_against_fp64(gpu_set, mod, L):
     y = dev(x)
     f.conv_batch(y, y, K)
     assert O.rel_l2(host(y), O.conv64(mod, x, h)) <= tol(mod, L)
+
+
+@pytest.mark.parametrize("mod,L", [(0, 131072), (1, 327680), (1, 393216), (0, 177147)])
+def test_three_level_group_order(fftset_lib, mod, L):
+    """Three-level task lists order the A and B tiles by n3 group and the
+    later B tiles and the C tiles by k1 group, B tiles waiting for their
+    n3 group's A tiles only, C tiles for their k1 group's B tiles. The
+    default lists every A tile first; a test hook interleaves the A and B
+    passes, the B tiles of a group following the A tiles of the group 1 or
+    2 slots later (a distance past the last group is the default). Every
+    order must list each tile once and give the same results bit for bit,
+    forward and inverse, batched."""
+    import ctypes as C
+    import torch
+    lib = fftset_lib.library()
+    lib.fftset__test_set_group_distance.restype = C.c_int
+    lib.fftset__test_set_group_distance.argtypes = [fftset_lib._P, C.c_uint]
+    rng = np.random.default_rng(L + 7 * mod)
+    x = torch.from_numpy(rng.standard_normal((3, 2 * L)).astype(np.float32)).cuda()
+    got = []
+    for dist in (0, 1, 2, 1000):
+        S = fftset_lib.FftSet()
+        try:
+            assert lib.fftset__test_set_group_distance(S.handle, dist) == 0
+            f = S.create_fft(mod, L)
+            X = torch.empty_like(x)
+            r = torch.empty_like(x)
+            f.forward_batch(X, x)
+            f.inverse_batch(r, X)
+            S.check()
+            got.append((X.cpu().numpy(), r.cpu().numpy()))
+        finally:
+            S.close()
+    xh = x.cpu().numpy()
+    assert O.rel_l2(got[0][0], O.forward64(mod, xh)) <= tol(mod, L)
+    for X, r in got[1:]:
+        assert np.array_equal(X, got[0][0]) and np.array_equal(r, got[0][1])
 
 
 def test_fourstep_large_single(gpu_set):
