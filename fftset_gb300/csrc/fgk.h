@@ -69,8 +69,10 @@ typedef struct fgk_plan4 {
 	uint32_t  L1, L2, modulation;
 	uint32_t  lshift1, lshift2;
 	uint32_t  threads1, threads2;
-	uint32_t  slots1, slots2;   /* shared float2 slots per CTA */
-	uint32_t  emax1, emax2;
+	uint32_t  slots1, slots2;   /* shared float2 slots of one tile buffer */
+	uint32_t  emax1, emax2;     /* 0: ping-pong tile (two buffers, one butterfly per
+	                             * thread at a time); else in place, up to emax
+	                             * points per thread in registers (one buffer) */
 	fgk_chain c1, c2;
 	const void *tw1, *tw2;      /* chain twiddles */
 	uint32_t  tshift;           /* w_L^m = thi[m >> tshift] * tlo[m & ((1 << tshift) - 1)] */

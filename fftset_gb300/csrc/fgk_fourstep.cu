@@ -28,6 +28,7 @@
 #include "fgk.h"
 #include "fgk_codelets.cuh"
 #include "fgk_pingpong.cuh"
+#include "fgk_tasks.cuh"
 
 namespace fgk {
 
@@ -148,6 +149,55 @@ __host__ __device__ __forceinline__ uint32_t lane_groups(uint32_t len, int nl, b
 	return mirror ? (((len + 1) >> 1) + (nl >> 1) - 1) / (nl >> 1) : (len + nl - 1) / nl;
 }
 
+/* Pass 1's input element n = L2 n1 + n2 (mode: FGK4_IN_*), with the
+ * FREQ_OFFSET_REAL modulation and pairing fused */
+__device__ __forceinline__ float2 pass1_load(const fgk_plan4 &p, int mode, const float *x, uint64_t L, uint64_t n,
+                                             uint32_t n1, uint32_t n2)
+{
+	const bool freq = p.modulation == FGK_MOD_FREQOFF;
+	if (mode == FGK4_IN_NATURAL)
+		return __ldcs(reinterpret_cast<const float2 *>(x) + n);
+	if (mode != FGK4_IN_INVERSE) {
+		if (freq) {
+			const float2 m = cmul(__ldg((const float2 *)p.m1 + n1), __ldg((const float2 *)p.m2 + n2));
+			return cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), m);
+		}
+		return __ldcs(reinterpret_cast<const float2 *>(x) + n);
+	}
+	const float2 *X = reinterpret_cast<const float2 *>(x);
+	if (freq) /* conj(W[n]): W[n] = X[2n] (n < ceil(L/2)), conj X[2(L-1-n)+1] otherwise */
+		return n < ((L + 1) >> 1) ? conjf2(__ldcs(X + 2 * n)) : __ldcs(X + 2 * (L - 1 - n) + 1);
+	return conjf2(__ldcs(X + n));
+}
+
+/* Pass 2's output of bin m = k1 + L1 k2 in every mode but the FREQ_OFFSET_REAL
+ * forward split (mode: FGK4_OUT_*) */
+__device__ __forceinline__ void pass2_store(const fgk_plan4 &p, int mode, float *o, uint64_t L, uint64_t m,
+                                            uint32_t k1, uint32_t k2, float2 v, const float *__restrict__ kern,
+                                            const int32_t *__restrict__ kidx, int kvw)
+{
+	if (mode == FGK4_OUT_KERNEL) {
+		/* spectrum bin m into the reference's kernel-buffer layout */
+		const int ko = __ldg(kidx + m);
+		o[ko] = v.x;
+		o[ko + kvw] = v.y;
+	} else if (mode == FGK4_OUT_PRODUCT || mode == FGK4_OUT_PRODUCT_CONJ) {
+		/* conj(W K) (or conj(W conj K)), natural order, for the second half of a convolution */
+		const int ko = __ldg(kidx + m);
+		const float2 k = make_float2(__ldg(kern + ko), __ldg(kern + ko + kvw));
+		__stcs(reinterpret_cast<float2 *>(o) + m, conjf2(mode == FGK4_OUT_PRODUCT ? cmul(v, k) : cmulc(v, k)));
+	} else if (mode == FGK4_OUT_FORWARD) {
+		__stcs(reinterpret_cast<float2 *>(o) + m, v);
+	} else if (p.modulation == FGK_MOD_FREQOFF) {
+		const float2 md = cmul(__ldg((const float2 *)p.n1 + k1), __ldg((const float2 *)p.n2 + k2));
+		const float2 r = cmul(v, md);
+		__stcs(o + m, r.x);
+		__stcs(o + L + m, r.y);
+	} else {
+		__stcs(reinterpret_cast<float2 *>(o) + m, conjf2(v));
+	}
+}
+
 /* Pass 1: columns. */
 template <int EMAX>
 __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int mode, const float *in, float2 *work,
@@ -180,27 +230,8 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass1(const fgk_plan4 p, int 
 		const int n1 = w >> t.lshift, lane = w & (t.nl - 1);
 		bool valid;
 		const uint32_t n2 = lane_index(grp, lane, t.nl, mirror, L2, valid);
-		float2 v = make_float2(0.f, 0.f);
-		if (valid) {
-			const uint64_t n = (uint64_t)L2 * n1 + n2;
-			if (mode == FGK4_IN_NATURAL) {
-				v = __ldcs(reinterpret_cast<const float2 *>(x) + n);
-			} else if (!inverse) {
-				if (freq) {
-					const float2 m = cmul(__ldg((const float2 *)p.m1 + n1), __ldg((const float2 *)p.m2 + n2));
-					v = cmul(make_float2(__ldcs(x + n), -__ldcs(x + L + n)), m);
-				} else {
-					v = __ldcs(reinterpret_cast<const float2 *>(x) + n);
-				}
-			} else {
-				const float2 *X = reinterpret_cast<const float2 *>(x);
-				if (freq) /* conj(W[n]): W[n] = X[2n] (n < ceil(L/2)), conj X[2(L-1-n)+1] otherwise */
-					v = n < ((L + 1) >> 1) ? conjf2(__ldcs(X + 2 * n)) : __ldcs(X + 2 * (L - 1 - n) + 1);
-				else
-					v = conjf2(__ldcs(X + n));
-			}
-		}
-		return v; }, [&](int w, float2 v) { t.st(w >> t.lshift, w & (t.nl - 1), v); });
+		return valid ? pass1_load(p, mode, x, L, (uint64_t)L2 * n1 + n2, (uint32_t)n1, n2) : make_float2(0.f, 0.f); },
+	    [&](int w, float2 v) { t.st(w >> t.lshift, w & (t.nl - 1), v); });
 	__syncthreads();
 	run_chain4<EMAX>(t, &dp->c1, (const float2 *)p.tw1);
 	for (int w = t.tid; w < items; w += t.T) {
@@ -283,28 +314,107 @@ __global__ void __launch_bounds__(512, 1) fourstep_pass2(const fgk_plan4 p, int 
 				__stcs(X + 2 * m + 1, conjf2(b));
 			continue;
 		}
-		const float2 v = t.ld(k2, lane);
-		if (mode == FGK4_OUT_KERNEL) {
-			/* spectrum bin m into the reference's kernel-buffer layout */
-			const int ko = __ldg(kidx + m);
-			o[ko] = v.x;
-			o[ko + kvw] = v.y;
-		} else if (mode == FGK4_OUT_PRODUCT || mode == FGK4_OUT_PRODUCT_CONJ) {
-			/* conj(W K) (or conj(W conj K)), natural order, for the second half of a convolution */
-			const int ko = __ldg(kidx + m);
-			const float2 k = make_float2(__ldg(kern + ko), __ldg(kern + ko + kvw));
-			__stcs(reinterpret_cast<float2 *>(o) + m, conjf2(mode == FGK4_OUT_PRODUCT ? cmul(v, k) : cmulc(v, k)));
-		} else if (forward) {
-			__stcs(reinterpret_cast<float2 *>(o) + m, v);
-		} else if (freq) {
-			const float2 md = cmul(__ldg((const float2 *)p.n1 + k1), __ldg((const float2 *)p.n2 + k2));
-			const float2 r = cmul(v, md);
-			__stcs(o + m, r.x);
-			__stcs(o + L + m, r.y);
-		} else {
-			__stcs(reinterpret_cast<float2 *>(o) + m, conjf2(v));
-		}
+		pass2_store(p, mode, o, L, m, k1, (uint32_t)k2, t.ld(k2, lane), kern, kidx, kvw);
 	}
+}
+
+/* ---- ping-pong tiles (plans with emax == 0) ------------------------------
+ * The tile's chain runs as in the task kernel (tile_chain, fgk_tasks.cuh):
+ * one butterfly per thread at a time between two padded shared-memory
+ * buffers, twiddles computed, no register batches and so no spills. */
+
+/* Pass 1: the first stage reads the input directly (the tile's NL columns
+ * are NL-element segments of each row), the last stage multiplies by
+ * w_L^{n2 k1} and writes the work buffer y[k1 L2 + n2]. */
+__global__ void __launch_bounds__(512, 1) fourstep_pp1(const fgk_plan4 p, int mode, const float *in, float2 *work,
+                                                        uint32_t count, size_t in_stride, size_t work_stride)
+{
+	extern __shared__ float2 smem[];
+	const int ls = (int)p.lshift1, nl = 1 << ls;
+	const uint32_t L1 = p.L1, L2 = p.L2;
+	const uint64_t L = (uint64_t)L1 * L2;
+	const bool mirror = p.modulation == FGK_MOD_FREQOFF && mode == FGK4_IN_INVERSE;
+	const uint32_t groups = lane_groups(L2, nl, mirror);
+	const uint64_t tr = blockIdx.x / groups;
+	const uint32_t grp = blockIdx.x - (uint32_t)(tr * groups);
+	if (tr >= count)
+		return;
+	const float *x = in + tr * in_stride;
+	float2 *y = work + tr * work_stride;
+	auto ld = [&](int n1, int lane) {
+		bool valid;
+		const uint32_t n2 = lane_index(grp, lane, nl, mirror, L2, valid);
+		return valid ? pass1_load(p, mode, x, L, (uint64_t)L2 * (uint32_t)n1 + n2, (uint32_t)n1, n2)
+		             : make_float2(0.f, 0.f);
+	};
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		bool valid;
+		const uint32_t n2 = lane_index(grp, lane, nl, mirror, L2, valid);
+		const uint32_t k1 = (uint32_t)(j + q * nbf);
+		if (valid)
+			__stcs(y + (uint64_t)k1 * L2 + n2, cmul(v, wl(p, (uint64_t)n2 * k1)));
+	};
+	tile_chain<false, Pad>(p.c1.code, (int)L1, ls, smem, smem + p.slots1, (int)threadIdx.x, (int)blockDim.x, true,
+	                       ld, st, [] {});
+}
+
+/* Pass 2: the tile's rows are copied into the second buffer first (a warp
+ * reads consecutive n2 of one row of the row-major work buffer), the first
+ * stage reads them there and writes the first buffer, the last stage writes
+ * the output directly. FREQ_OFFSET_REAL forward: lanes NL/2.. hold the
+ * mirror rows, so both halves of every 16-byte bin pair come from this CTA. */
+__global__ void __launch_bounds__(512, 1) fourstep_pp2(const fgk_plan4 p, int mode, const float2 *work, float *out,
+                                                        uint32_t count, size_t work_stride, size_t out_stride,
+                                                        const float *__restrict__ kern,
+                                                        const int32_t *__restrict__ kidx, int kvw)
+{
+	extern __shared__ float2 smem[];
+	const int ls = (int)p.lshift2, nl = 1 << ls;
+	const uint32_t L1 = p.L1, L2 = p.L2;
+	const uint64_t L = (uint64_t)L1 * L2;
+	const bool mirror = p.modulation == FGK_MOD_FREQOFF && mode == FGK4_OUT_FORWARD;
+	const uint32_t groups = lane_groups(L1, nl, mirror);
+	const uint64_t tr = blockIdx.x / groups;
+	const uint32_t grp = blockIdx.x - (uint32_t)(tr * groups);
+	if (tr >= count)
+		return;
+	const float2 *yin = work + tr * work_stride;
+	float *o = out + tr * out_stride;
+	float2 *A = smem, *B = smem + p.slots2;
+	const Pad ad{ls};
+	batched_copy<8>(
+	    (int)L2 << ls, (int)threadIdx.x, (int)blockDim.x,
+	    [&](int w) {
+		    const int lane = w / (int)L2, n2 = w - lane * (int)L2;
+		    bool valid;
+		    const uint32_t k1 = lane_index(grp, lane, nl, mirror, L1, valid);
+		    return valid ? __ldcs(yin + (uint64_t)k1 * L2 + n2) : make_float2(0.f, 0.f);
+	    },
+	    [&](int w, float2 v) {
+		    const int lane = w / (int)L2, n2 = w - lane * (int)L2;
+		    B[ad.slot(n2, lane)] = v;
+	    });
+	__syncthreads();
+	auto ld = [&](int n2, int lane) { return B[ad.slot(n2, lane)]; };
+	auto st = [&](int j, int q, int nbf, int lane, float2 v) {
+		bool valid;
+		const uint32_t k1 = lane_index(grp, lane, nl, mirror, L1, valid);
+		if (!valid)
+			return;
+		const uint32_t k2 = (uint32_t)(j + q * nbf);
+		const uint64_t m = k1 + (uint64_t)L1 * k2;
+		if (mirror) {
+			/* X[2m] = W[m] for m < ceil(L/2); otherwise W[m] = conj X[2(L-1-m)+1] */
+			float2 *X = reinterpret_cast<float2 *>(o);
+			if (m < ((L + 1) >> 1))
+				__stcs(X + 2 * m, v);
+			else
+				__stcs(X + 2 * (L - 1 - m) + 1, conjf2(v));
+		} else {
+			pass2_store(p, mode, o, L, m, k1, k2, v, kern, kidx, kvw);
+		}
+	};
+	tile_chain<false, Pad>(p.c2.code, (int)L2, ls, A, B, (int)threadIdx.x, (int)blockDim.x, true, ld, st, [] {});
 }
 
 } /* namespace fgk */
@@ -318,9 +428,11 @@ static int launch_pass(const fgk_plan4 *p, int in_mode, int out_mode, float *out
 	const int nl1 = 1 << p->lshift1, nl2 = 1 << p->lshift2;
 	const uint32_t g1 = lane_groups(p->L2, nl1, freq && in_mode == FGK4_IN_INVERSE);
 	const uint32_t g2 = lane_groups(p->L1, nl2, freq && out_mode == FGK4_OUT_FORWARD);
-	const size_t sm1 = (size_t)p->slots1 * sizeof(float2), sm2 = (size_t)p->slots2 * sizeof(float2);
-	auto k1 = p->emax1 > 16 ? fourstep_pass1<32> : fourstep_pass1<16>;
-	auto k2 = p->emax2 > 16 ? fourstep_pass2<32> : fourstep_pass2<16>;
+	/* ping-pong tiles hold two buffers */
+	const size_t sm1 = (size_t)p->slots1 * sizeof(float2) * (p->emax1 ? 1 : 2);
+	const size_t sm2 = (size_t)p->slots2 * sizeof(float2) * (p->emax2 ? 1 : 2);
+	auto k1 = p->emax1 == 0 ? fourstep_pp1 : p->emax1 > 16 ? fourstep_pass1<32> : fourstep_pass1<16>;
+	auto k2 = p->emax2 == 0 ? fourstep_pp2 : p->emax2 > 16 ? fourstep_pass2<32> : fourstep_pass2<16>;
 	cudaError_t e;
 	if ((e = cudaFuncSetAttribute((const void *)k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1)) != cudaSuccess)
 		return (int)e;

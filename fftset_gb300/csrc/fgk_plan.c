@@ -267,10 +267,32 @@ static int plan_pass(uint32_t Lp, int mirror, uint32_t max_smem, fgk_chain *ch, 
 	uint32_t rad[FGK_MAX_STAGES], n, ls, emax;
 	if (fgk_plan_chain(Lp, rad, &n))
 		return -1;
-	/* widest lane count (<= 16) whose tile fits half the shared memory (two
-	 * CTAs per SM) and whose stages fit 512 threads; below 4 lanes the HBM
-	 * segments get narrower than a 32-byte sector, so 4 lanes may take the
-	 * whole shared memory */
+	/* ping-pong tiles (two buffers, no register batches, so no spills): the
+	 * widest lane count (<= 16) whose two buffers fit half the shared memory
+	 * (two CTAs per SM), or at most 4 lanes in the whole of it; threads: the
+	 * widest stage's butterflies, 128 to 512; chains of up to 15 stages */
+	for (ls = 4; n <= 15; ls--) {
+		const uint32_t nl = 1u << ls, sl = (Lp * nl + (Lp * nl) / 16 + 1 + 3) & ~3u;
+		if ((size_t)2 * sl * 8 <= max_smem / 2 || (ls <= 2 && (size_t)2 * sl * 8 <= max_smem)) {
+			uint32_t s, T = 128;
+			for (s = 0; s < n; s++)
+				if (Lp / rad[s] * nl > T)
+					T = Lp / rad[s] * nl;
+			T = T > 512 ? 512 : (T + 31) & ~31u;
+			*threads = T;
+			*emax_out = 0;
+			*slots = sl;
+			*lshift = ls;
+			fill_chain(ch, rad, n, Lp, T);
+			return 0;
+		}
+		if (ls == (mirror ? 1u : 0u))
+			break;
+	}
+	/* otherwise in place: the widest lane count (<= 16) whose tile fits
+	 * half the shared memory (two CTAs per SM) and whose stages fit 512
+	 * threads; below 4 lanes the HBM segments get narrower than a 32-byte
+	 * sector, so 4 lanes may take the whole shared memory */
 	for (ls = 4;; ls--) {
 		uint32_t nl = 1u << ls, sl = Lp * nl + (Lp * nl) / 16 + 1;
 		int ok = 0;

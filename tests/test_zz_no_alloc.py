@@ -47,7 +47,11 @@ def fset(fftset_lib):
     s.close()
 
 
-@pytest.mark.parametrize("mod,L,count", [(0, 32768, 4), (1, 36864, 3), (1, 65536, 2)])
+# 59049 = 243 x 243 and 177147 = 243 x 729: odd factors (a self-mirrored
+# middle row or column in the FREQ_OFFSET_REAL pairing); 1048576: four-lane
+# tiles of 1024 points
+@pytest.mark.parametrize("mod,L,count", [(0, 32768, 4), (1, 36864, 3), (1, 65536, 2), (1, 59049, 2),
+                                         (1, 177147, 2), (0, 131072, 2), (1, 1048576, 2)])
 def test_fixed_scratch_matches_batched_call(fftset_lib, fset, mod, L, count):
     import torch
     fn = _entry(fftset_lib)
