@@ -10,7 +10,11 @@
  * transform). A CTA owns NL transforms of one
  * pass (NL adjacent columns, or NL adjacent rows) and keeps them lane-
  * interleaved in shared memory (element i of lane l at slot(i NL + l)), so
- * its HBM accesses are NL-element contiguous segments.
+ * its HBM accesses are NL-element contiguous segments. Two forms, chosen by
+ * the planner (fgk_plan4.emax): ping-pong tiles (fourstep_pp1/2: two
+ * buffers, the chain run as the task kernel runs it, tile_chain) wherever
+ * two buffers fit, else in place (fourstep_pass1/2: one buffer, each
+ * stage's points read into registers, a barrier, then written back).
  *
  * The modulation edges of the reference are fused as in the resident path:
  *   FREQ_OFFSET_REAL forward: pass 1 loads c[n] = conj(x[n] + j x[L+n])
