@@ -460,6 +460,28 @@ def test_three_level_group_order(fftset_lib, mod, L):
         assert np.array_equal(X, got[0][0]) and np.array_equal(r, got[0][1])
 
 
+@pytest.mark.parametrize("mod", [0, 1])
+def test_beyond_three_levels(gpu_set, mod):
+    """2^25 bins has no three-level split (a factor above 256), so the
+    two-pass kernels run it: ping-pong tiles, and for the FREQ_OFFSET_REAL
+    forward's rows of 8192 points (two tile buffers do not fit) the
+    in-place form. Forward against FP64, and the round trip."""
+    import torch
+    L = 1 << 25
+    f = gpu_set.create_fft(mod, L)
+    assert f is not None
+    rng = np.random.default_rng(25 + mod)
+    x = rng.standard_normal((1, 2 * L)).astype(np.float32)
+    X = torch.empty(1, 2 * L, device="cuda")
+    f.forward_batch(X, dev(x))
+    Xh = host(X)
+    assert O.rel_l2(Xh, O.forward64(mod, x)) <= tol(mod, L)
+    r = torch.empty_like(X)
+    f.inverse_batch(r, X)
+    assert O.rel_l2(host(r) / L, x) <= 2 * tol(mod, L)
+    gpu_set.check()
+
+
 def test_fourstep_large_single(gpu_set):
     """The 15,728,640-bin FREQ_OFFSET_REAL transform: forward against FP64
     (error per bin band) and the forward/inverse round trip."""
