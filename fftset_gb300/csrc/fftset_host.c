@@ -686,7 +686,7 @@ static int fs_pick_variant(const struct fftset_fft *f, int op, unsigned count)
 	return f->sel[op];
 }
 
-/* no_bulk: the buffers live in host memory, which this build does not read
+/* no_bulk: the buffers live in host memory, which the library does not read
  * with bulk copies (TMA): variants with bulk-copy input are skipped */
 static int fs_launch_variant_ex(const struct fftset_fft *f, int v, int op, float *out, const float *in,
                                 const float *kern, unsigned count, size_t in_stride, size_t out_stride,

@@ -1,8 +1,8 @@
 /* ORACLE TEST INFRASTRUCTURE -- not part of the product.
  *
  * CPU restatement of fftset's transform and fast-convolution path
- * (templeblock/fftset), used only by tests/, by __graft_entry__.smoke() as the
- * checker, and by bench.py as the timed CPU baseline ("port"). It follows the
+ * (templeblock/fftset), used only by tests/, by __graft_entry__.smoke() to
+ * check its results, and by bench.py as the timed CPU baseline ("port"). It follows the
  * reference algorithm step by step:
  *
  *   planner          src/fftset_vec.c:945-971 (radix table), :1004-1062
