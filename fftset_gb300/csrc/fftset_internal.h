@@ -194,6 +194,11 @@ int  fftset__test_set_task_shape(struct fftset *fc, int shape);
  * lists of later ragged creates (0: the default, every A tile first) */
 int  fftset__test_set_group_distance(struct fftset *fc, unsigned slots);
 int  fftset__test_ragged_drop_kind(struct fftset_ragged *rb, int kind);
+/* the task order of one three-level item L1 x L2 x L3 (fftset_ragged.c,
+ * fsr_list_huge), written to out (at most cap tasks; returns the count,
+ * 0 when cap is too small); no GPU is involved */
+uint32_t fftset__test_list_huge(uint32_t L1, uint32_t L2, uint32_t L3, int zip_in, int zip_out, uint32_t grid,
+                                uint32_t group_dist, fgk_task *out, uint32_t cap);
 #if !defined(FS_ALLOC_IMPL) && !defined(__cplusplus)
 #include <stdlib.h>
 #define malloc(n)                 fs_malloc(n)

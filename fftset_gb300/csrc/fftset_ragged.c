@@ -103,6 +103,140 @@ static uint32_t fsr_lanes_log2(uint32_t lp, uint32_t count)
 	return ls;
 }
 
+/* tile counts of a three-level item L1 x L2 x L3 (fgk_huge): A tiles of 16
+ * columns, B tiles of 4 x 4 (k1, n3) blocks, C tiles of 16 k1; A and B
+ * tiles in L3/16 groups by n3 when 16 divides L3 */
+static void fsr_huge_tiles(fgk_huge *h, uint32_t L1, uint32_t L2, uint32_t L3)
+{
+	h->L1 = L1;
+	h->L2 = L2;
+	h->L3 = L3;
+	h->ngrp = L3 % 16 == 0 ? L3 / 16 : 1;
+	h->reserved = 0;
+	h->na = (L2 * L3 + 15) / 16;
+	h->nb3 = (L3 + 3) / 4;
+	h->nb = (L1 + 3) / 4 * h->nb3;
+	h->nc1 = (L1 + 15) / 16;
+}
+
+/* the k-th of N tiles listed next to its mirror: 0, N-1, 1, N-2, ... */
+static uint32_t fsr_zip(int on, uint32_t k, uint32_t N)
+{
+	return on ? ((k & 1) ? N - 1 - (k >> 1) : k >> 1) : k;
+}
+
+/* The tasks of three-level item i (ref i). A tiles slot by slot, a slot
+ * being one n3 group of L2 A tiles (tile t = n2 ngrp + u for group u), or
+ * with mirror tiles adjacent the pair of groups u and ngrp-1-u (the mirror
+ * of tile (u, n2) is (ngrp-1-u, L2-1-n2)). Then the B tiles of the first P
+ * slots in the same order: at the A -> B boundary only the groups of the
+ * last A tiles are still running, and these B tiles belong to groups
+ * finished long before, so they start at once instead of waiting for the
+ * whole pass. Then the other slots' B tiles by k1 group of 16 (P slots hold
+ * about two grids of B tiles, so every A tile is done by then), and the C
+ * tiles by k1 group in the same order: at the B -> C boundary the first C
+ * tiles belong to k1 groups finished long before. With one n3 group the B
+ * tiles are listed in index order, which is k1 order. The mirror of C tile
+ * (k2, g) is (L2-1-k2, nc1-1-g): with mirror tiles adjacent the k1 groups
+ * go in pairs g, nc1-1-g. Every tile is listed after the tiles it waits
+ * for, so no wait depends on a tile not yet claimed.
+ * 15,728,640 bins forward + inverse: 0.535 ms with every A tile before
+ * every B tile and every B tile before every C tile; 0.516 with the A -> B
+ * boundary opened, 0.496-0.500 with both. group_dist interleaves the A and
+ * B passes instead (a test hook sets it), the B tiles of slot s after the
+ * A tiles of slot s + D: that measured slower (D = 2: 0.552 ms; D = 9:
+ * 0.524 ms), the interleaved B tiles waiting on A tiles still in flight.
+ * Returns the tasks written: na + nb + nc1 L2. */
+static uint32_t fsr_list_huge(fgk_task *tasks, uint32_t i, const fgk_huge *h, int zip_in, int zip_out, uint32_t grid,
+                              uint32_t group_dist)
+{
+	uint32_t ntasks = 0;
+	const uint32_t U = h->ngrp, L2 = h->L2, L1q = h->nb / h->nb3, nc1 = h->nc1;
+	const uint32_t nslot = U > 1 && zip_in ? (U + 1) / 2 : U;
+	const uint32_t D = group_dist && group_dist < nslot ? group_dist : nslot;
+	const uint32_t per_b = (U > 1 && zip_in ? 8 : 4) * L1q; /* B tiles of a slot */
+	const uint32_t P = U == 1 ? 0 : D < nslot ? nslot : (2 * grid + per_b - 1) / per_b;
+	uint32_t s, t, k, q;
+	for (s = 0; s < nslot + D; s++) {
+		if (s < nslot) {
+			const uint32_t u0 = s, u1 = U - 1 - s;
+			if (U == 1)
+				for (t = 0; t < h->na; t++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, fsr_zip(zip_in, t, h->na), 0};
+			else if (!zip_in)
+				for (k = 0; k < L2; k++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, k * U + u0, 0};
+			else if (u0 != u1)
+				for (k = 0; k < 2 * L2; k++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i,
+					                             k & 1 ? (L2 - 1 - (k >> 1)) * U + u1 : (k >> 1) * U + u0, 0};
+			else
+				for (k = 0; k < L2; k++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, fsr_zip(1, k, L2) * U + u0, 0};
+		}
+		if (s >= D && s - D < P) {
+			/* the slot's groups, their 4 n3 blocks for every k1 block:
+			 * t = k1 block x nb3 + n3 block */
+			const uint32_t u0 = s - D, u1 = U - 1 - (s - D);
+			for (q = 0; q < (zip_in && u1 != u0 ? 2u : 1u); q++)
+				for (k = 0; k < L1q * 4; k++)
+					tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, (k >> 2) * h->nb3 + 4 * (q ? u1 : u0) + (k & 3),
+					                             0};
+		}
+	}
+	/* k1 groups in C's order: g = 0, 1, ... or the pairs g, nc1-1-g */
+	for (k = 0; k < (zip_out ? (nc1 + 1) / 2 : nc1); k++) {
+		const uint32_t g0 = k, g1 = zip_out ? nc1 - 1 - k : k;
+		uint32_t g;
+		for (g = g0;; g = g1) {
+			const uint32_t b1 = 4 * g + 4 < L1q ? 4 * g + 4 : L1q;
+			uint32_t b, j;
+			if (U == 1) {
+				for (b = 4 * g; b < b1; b++)
+					for (j = 0; j < h->nb3; j++)
+						tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, b * h->nb3 + j, 0};
+			} else {
+				for (s = P; s < nslot; s++) {
+					const uint32_t u0 = s, u1 = U - 1 - s;
+					for (q = 0; q < (zip_in && u1 != u0 ? 2u : 1u); q++)
+						for (b = 4 * g; b < b1; b++)
+							for (j = 0; j < 4; j++)
+								tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, b * h->nb3 + 4 * (q ? u1 : u0) + j, 0};
+				}
+			}
+			if (g == g1)
+				break;
+		}
+	}
+	for (k = 0; k < (zip_out ? (nc1 + 1) / 2 : nc1); k++) {
+		const uint32_t g0 = k, g1 = zip_out ? nc1 - 1 - k : k;
+		if (g0 == g1)
+			for (t = 0; t < L2; t++)
+				tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i, fsr_zip(zip_out, t, L2) * nc1 + g0, 0};
+		else
+			for (t = 0; t < 2 * L2; t++)
+				tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i,
+				                             t & 1 ? (L2 - 1 - (t >> 1)) * nc1 + g1 : (t >> 1) * nc1 + g0, 0};
+	}
+	return ntasks;
+}
+
+/* Test hook: the task order of one three-level item L1 x L2 x L3 (ref 0),
+ * mirror tiles adjacent on the input (zip_in) or the output (zip_out) side,
+ * for a grid of `grid` CTAs and A -> B distance group_dist (0: every A tile
+ * first); returns the tasks written, 0 when cap is too small. No GPU is
+ * involved. */
+uint32_t fftset__test_list_huge(uint32_t L1, uint32_t L2, uint32_t L3, int zip_in, int zip_out, uint32_t grid,
+                                uint32_t group_dist, fgk_task *out, uint32_t cap)
+{
+	fgk_huge h;
+	memset(&h, 0, sizeof(h));
+	fsr_huge_tiles(&h, L1, L2, L3);
+	if ((uint64_t)h.na + h.nb + (uint64_t)h.nc1 * L2 > cap)
+		return 0;
+	return fsr_list_huge(out, 0, &h, zip_in, zip_out, grid, group_dist);
+}
+
 void fsr_free(struct fftset_ragged *rb)
 {
 	if (!rb)
@@ -239,13 +373,8 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 				/* each scratch area in 4 x 4 blocks: L2 ceil(L1/4) ceil(L3/4) x 16 */
 				const size_t span = (size_t)p3->L2 * ((p3->L1 + 3) / 4) * ((p3->L3 + 3) / 4) * 16;
 				h->p3 = p3->dev;
-				h->L1 = p3->L1;
-				h->L2 = p3->L2;
-				h->L3 = p3->L3;
-				/* A and B tiles in L3/16 groups by n3 when 16 divides L3 */
-				h->ngrp = p3->L3 % 16 == 0 ? p3->L3 / 16 : 1;
+				fsr_huge_tiles(h, p3->L1, p3->L2, p3->L3);
 				h->cnt = nhcount;
-				h->reserved = 0;
 				h->code1 = p3->c1.code;
 				h->code2 = p3->c2.code;
 				h->code3 = p3->c3.code;
@@ -254,10 +383,6 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 				h->sa = scratch_f2;
 				h->sb = scratch_f2 + span;
 				scratch_f2 += 2 * span;
-				h->na = (p3->L2 * p3->L3 + 15) / 16;
-				h->nb3 = (p3->L3 + 3) / 4;
-				h->nb = (p3->L1 + 3) / 4 * h->nb3;
-				h->nc1 = (p3->L1 + 15) / 16;
 				nhcount += h->ngrp + h->nc1;
 				cap_tasks += h->na + h->nb + h->nc1 * p3->L2;
 			}
@@ -331,98 +456,10 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 	 * sectors instead of two partial writes (or reads) far apart. */
 	const int zip_in = rb->modulation == FGK_MOD_FREQOFF && op == FFTSET_OP_INVERSE;
 	const int zip_out = rb->modulation == FGK_MOD_FREQOFF && op == FFTSET_OP_FORWARD;
-#define FSR_ZIP(on, k, N) ((on) ? (((k) & 1) ? (N) - 1 - ((k) >> 1) : ((k) >> 1)) : (k))
-	/* three-level items. A tiles slot by slot, a slot being one n3 group
-	 * of L2 A tiles (tile t = n2 ngrp + u for group u), or with mirror
-	 * tiles adjacent the pair of groups u and ngrp-1-u (the mirror of tile
-	 * (u, n2) is (ngrp-1-u, L2-1-n2)). Then the B tiles of the first P
-	 * slots in the same order: at the A -> B boundary only the groups of
-	 * the last A tiles are still running, and these B tiles belong to
-	 * groups finished long before, so they start at once instead of
-	 * waiting for the whole pass. Then the other slots' B tiles by k1 group
-	 * of 16 (P slots hold about two grids of B tiles, so every A tile is
-	 * done by then), and the C tiles by k1 group in the same order: at the
-	 * B -> C boundary the first C tiles belong to k1 groups finished long
-	 * before. With one n3 group the B tiles are listed in index order,
-	 * which is k1 order. The mirror of C tile (k2, g) is (L2-1-k2, nc1-1-g):
-	 * with mirror tiles adjacent the k1 groups go in pairs g, nc1-1-g.
-	 * 15,728,640 bins forward + inverse: 0.535 ms with every A tile before
-	 * every B tile and every B tile before every C tile; 0.516 with the
-	 * A -> B boundary opened, 0.496-0.500 with both. A test hook interleaves the passes instead,
-	 * the B tiles of slot s after the A tiles of slot s + D: that measured
-	 * slower (D = 2: 0.552 ms; D = 9: 0.524 ms), the interleaved B tiles
-	 * waiting on A tiles still in flight. */
-	for (i = 0; i < nhuge; i++) {
-		const fgk_huge *h = &huges[i];
-		const uint32_t U = h->ngrp, L2 = h->L2, L1q = h->nb / h->nb3, nc1 = h->nc1;
-		const uint32_t nslot = U > 1 && zip_in ? (U + 1) / 2 : U;
-		const uint32_t D = fs->group_dist && fs->group_dist < nslot ? fs->group_dist : nslot;
-		const uint32_t grid = (uint32_t)fgk_tasks_grid(fs->num_sms, rb->shape);
-		const uint32_t per_b = (U > 1 && zip_in ? 8 : 4) * L1q; /* B tiles of a slot */
-		const uint32_t P = U == 1 ? 0 : D < nslot ? nslot : (2 * grid + per_b - 1) / per_b;
-		uint32_t s, t, k, q;
-		for (s = 0; s < nslot + D; s++) {
-			if (s < nslot) {
-				const uint32_t u0 = s, u1 = U - 1 - s;
-				if (U == 1)
-					for (t = 0; t < h->na; t++)
-						tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, FSR_ZIP(zip_in, t, h->na), 0};
-				else if (!zip_in)
-					for (k = 0; k < L2; k++)
-						tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, k * U + u0, 0};
-				else if (u0 != u1)
-					for (k = 0; k < 2 * L2; k++)
-						tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i,
-						                             k & 1 ? (L2 - 1 - (k >> 1)) * U + u1 : (k >> 1) * U + u0, 0};
-				else
-					for (k = 0; k < L2; k++)
-						tasks[ntasks++] = (fgk_task){FGK_TASK_PA, i, FSR_ZIP(1, k, L2) * U + u0, 0};
-			}
-			if (s >= D && s - D < P) {
-				/* the slot's groups, their 4 n3 blocks for every k1 block:
-				 * t = k1 block x nb3 + n3 block */
-				const uint32_t u0 = s - D, u1 = U - 1 - (s - D);
-				for (q = 0; q < (zip_in && u1 != u0 ? 2u : 1u); q++)
-					for (k = 0; k < L1q * 4; k++)
-						tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, (k >> 2) * h->nb3 + 4 * (q ? u1 : u0) + (k & 3),
-						                             0};
-			}
-		}
-		/* k1 groups in C's order: g = 0, 1, ... or the pairs g, nc1-1-g */
-		for (k = 0; k < (zip_out ? (nc1 + 1) / 2 : nc1); k++) {
-			const uint32_t g0 = k, g1 = zip_out ? nc1 - 1 - k : k;
-			uint32_t g;
-			for (g = g0;; g = g1) {
-				const uint32_t b1 = 4 * g + 4 < L1q ? 4 * g + 4 : L1q;
-				uint32_t b, j;
-				if (U == 1) {
-					for (b = 4 * g; b < b1; b++)
-						for (j = 0; j < h->nb3; j++)
-							tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, b * h->nb3 + j, 0};
-				} else {
-					for (s = P; s < nslot; s++) {
-						const uint32_t u0 = s, u1 = U - 1 - s;
-						for (q = 0; q < (zip_in && u1 != u0 ? 2u : 1u); q++)
-							for (b = 4 * g; b < b1; b++)
-								for (j = 0; j < 4; j++)
-									tasks[ntasks++] = (fgk_task){FGK_TASK_PB, i, b * h->nb3 + 4 * (q ? u1 : u0) + j, 0};
-					}
-				}
-				if (g == g1)
-					break;
-			}
-		}
-		for (k = 0; k < (zip_out ? (nc1 + 1) / 2 : nc1); k++) {
-			const uint32_t g0 = k, g1 = zip_out ? nc1 - 1 - k : k;
-			if (g0 == g1)
-				for (t = 0; t < L2; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i, FSR_ZIP(zip_out, t, L2) * nc1 + g0, 0};
-			else
-				for (t = 0; t < 2 * L2; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_PC, i,
-					                             t & 1 ? (L2 - 1 - (t >> 1)) * nc1 + g1 : (t >> 1) * nc1 + g0, 0};
-		}
-	}
+	/* three-level items: the order is described at fsr_list_huge */
+	for (i = 0; i < nhuge; i++)
+		ntasks += fsr_list_huge(tasks + ntasks, i, &huges[i], zip_in, zip_out,
+		                        (uint32_t)fgk_tasks_grid(fs->num_sms, rb->shape), fs->group_dist);
 	/* big items: COLS of item b, ROWS of item b - D */
 	if (nbig) {
 		const uint64_t grid = (uint64_t)fgk_tasks_grid(fs->num_sms, rb->shape);
@@ -431,13 +468,12 @@ static struct fftset_ragged *fsr_create(struct fs_impl *fs, const struct fftset_
 		for (b = 0; b < nbig + D; b++) {
 			if (b < nbig)
 				for (t = 0; t < bigs[b].ncols; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_COLS, b, FSR_ZIP(zip_in, t, bigs[b].ncols), 0};
+					tasks[ntasks++] = (fgk_task){FGK_TASK_COLS, b, fsr_zip(zip_in, t, bigs[b].ncols), 0};
 			if (b >= D)
 				for (t = 0; t < bigs[b - D].nrows; t++)
-					tasks[ntasks++] = (fgk_task){FGK_TASK_ROWS, b - D, FSR_ZIP(zip_out, t, bigs[b - D].nrows), 0};
+					tasks[ntasks++] = (fgk_task){FGK_TASK_ROWS, b - D, fsr_zip(zip_out, t, bigs[b - D].nrows), 0};
 		}
 	}
-#undef FSR_ZIP
 	/* small items, largest first */
 	{
 		uint32_t pi = 0;
