@@ -625,13 +625,19 @@ def run_gb300(args):
     xh = torch.from_numpy(x_np).pin_memory()
     yh = torch.empty_like(xh).pin_memory()
     f.conv_batch(yh, xh, K)
-    e2e_steps = max(3, min(args.steps, 20))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        f.conv_batch(yh, xh, K)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world)
+    # three timed blocks of steps, the median reported: the host link is
+    # shared with the machine's other work, and one full run read 18 % low
+    # with the device-side step unchanged
+    e2e_block = max(1, min(args.steps, 21) // 3)
+    e2e_blocks = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_block):
+            f.conv_batch(yh, xh, K)
+        torch.cuda.synchronize()
+        e2e_blocks.append(max_over_ranks((time.perf_counter() - t0) / e2e_block, world))
+    e2e_s = sorted(e2e_blocks)[1]
     e2e_ok = O.rel_l2(yh[:nchk].numpy(), y_ref) <= O.tolerance(2 * L)
 
     peak, peak_kind = measured_peak()
@@ -663,7 +669,8 @@ def run_gb300(args):
             "cpu_baseline": cb,
             "e2e": {"value": job_gbs(world, e2e_s), "unit": "GB/s",
                     "h2d_bytes_per_step": int(x_np.nbytes), "d2h_bytes_per_step": int(x_np.nbytes),
-                    "parity_ok": bool(e2e_ok)},
+                    "parity_ok": bool(e2e_ok), "steps_per_block": e2e_block,
+                    "blocks_gbs": [job_gbs(world, t) for t in e2e_blocks], "reported": "median of the blocks"},
             "gpu_launches": launches,
             "clocks": clocks,
             "remeasured": remeasured,
