@@ -73,3 +73,34 @@ def test_three_level_splits(lib, L):
     for f in (L1, L2, L3):
         rc, rad = _chain(lib, f)
         assert rc == 0 and math.prod(rad) == f
+
+
+@pytest.mark.parametrize("mod", [0, 1])
+@pytest.mark.parametrize("L", [32768, 59049, 65536, 131072, 177147, 393216, 1 << 20, 15728640, 1 << 24, 1 << 25,
+                               3 ** 15])
+def test_two_pass_tiles(lib, mod, L):
+    """The tiles of the two-pass kernels (get_kernel beyond the resident
+    limit, the fixed-scratch entry point, sizes beyond the three-level
+    range): ping-pong tiles (emax 0, two buffers) wherever two buffers fit
+    the shared memory, else in place (one buffer, emax 16 or 32); lane
+    counts of at most 16, at least 2 for the FREQ_OFFSET_REAL passes that
+    hold mirror rows (forward pass 2, inverse pass 1), threads a multiple
+    of 32 up to 512."""
+    if not O.valid_size(L):
+        pytest.skip("not a supported size")
+    buf = (C.c_uint32 * 8192)()
+    assert lib.fgk_plan_fourstep(buf, C.c_uint32(L), C.c_uint32(mod), C.c_uint32(SMEM)) == 0
+    L1, L2 = buf[0], buf[1]
+    assert L1 * L2 == L
+    for Lp, ls, T, slots, emax in ((L1, buf[3], buf[5], buf[7], buf[9]), (L2, buf[4], buf[6], buf[8], buf[10])):
+        nl = 1 << ls
+        assert ls <= 4 and (mod == 0 or ls >= 1), (Lp, ls)
+        assert slots >= Lp * nl + (Lp * nl) // 16 + 1, (Lp, slots)
+        assert 32 <= T <= 512 and T % 32 == 0, (Lp, T)
+        if emax == 0:
+            assert 2 * slots * 8 <= SMEM and slots % 4 == 0, (Lp, slots)
+        else:
+            assert emax in (16, 32) and slots * 8 <= SMEM, (Lp, emax, slots)
+            # in place only where two buffers of the narrowest allowed tile do not fit
+            nl_min = 2 if mod else 1
+            assert 2 * (Lp * nl_min + (Lp * nl_min) // 16 + 1) * 8 > SMEM, (Lp, emax)
